@@ -1,0 +1,426 @@
+// capi.cu -- the extern "C" boundary of mesoengine_gb300 (declared in
+// include/meso.h): context, device memory/stream/event helpers, scenes,
+// meshing and raymarching entry points.  No exception crosses this layer;
+// every failure becomes a meso_status plus a per-thread message.
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "meso_internal.h"
+
+namespace meso {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string& msg) { g_err = msg; }
+
+meso_status fail(meso_status s, const std::string& msg) {
+  g_err = msg;
+  return s;
+}
+
+meso_status cuda_fail(cudaError_t e, const char* what) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? MESO_ERR_OOM : MESO_ERR_CUDA;
+}
+
+// defined in scene.cu
+meso_status scene_create_terrain(meso_ctx*, const meso_terrain*, uint64_t, meso_scene**);
+meso_status scene_create_dense(meso_ctx*, const uint16_t*, int32_t, int32_t, int32_t, uint64_t, meso_scene**);
+meso_status generate_dense_u8(meso_ctx*, int32_t, int32_t, int32_t, uint32_t, uint8_t*, cudaStream_t);
+meso_status generate_chunks_u16(meso_ctx*, uint32_t, uint32_t, uint16_t*, uint32_t*, cudaStream_t);
+meso_status edit_spheres(meso_ctx*, meso_scene*, const meso_sphere_edit*, uint32_t, uint32_t*, uint32_t, uint32_t*,
+                         cudaStream_t);
+
+// Minimal reader for the tuning JSON written by meso_autotune: flat
+// {"key": number, ...}.
+static void load_tuning(const char* path, Tuning& t) {
+  if (!path || !*path) return;
+  std::ifstream f(path);
+  if (!f) return;
+  std::stringstream ss;
+  ss << f.rdbuf();
+  const std::string s = ss.str();
+  auto num = [&](const char* key, uint32_t& dst) {
+    const std::string k = std::string("\"") + key + "\"";
+    size_t p = s.find(k);
+    if (p == std::string::npos) return;
+    p = s.find(':', p);
+    if (p == std::string::npos) return;
+    long v = strtol(s.c_str() + p + 1, nullptr, 10);
+    if (v > 0 && v < 1 << 20) dst = (uint32_t)v;
+  };
+  num("mesh_ctas_per_sm", t.mesh_ctas_per_sm);
+  num("mesh_chunks_per_ticket", t.mesh_chunks_per_ticket);
+  num("ray_tile_w", t.ray_tile_w);
+  num("ray_warps_per_cta", t.ray_warps_per_cta);
+}
+
+}  // namespace meso
+
+using namespace meso;
+
+extern "C" {
+
+const char* meso_last_error_string(void) { return g_err.c_str(); }
+
+const char* meso_status_string(meso_status s) {
+  switch (s) {
+    case MESO_OK: return "ok";
+    case MESO_ERR_INVALID_ARG: return "invalid argument";
+    case MESO_ERR_OOM: return "out of memory";
+    case MESO_ERR_OVER_BUDGET: return "over HBM budget";
+    case MESO_ERR_OVERFLOW: return "output overflow";
+    case MESO_ERR_TIMEOUT: return "device wait timed out";
+    case MESO_ERR_CUDA: return "CUDA error";
+    case MESO_ERR_NOT_READY: return "not ready";
+    case MESO_ERR_SHUTDOWN: return "shut down";
+  }
+  return "unknown";
+}
+
+meso_status meso_ctx_create(const meso_config* cfg, meso_ctx** out) {
+  if (!out) return fail(MESO_ERR_INVALID_ARG, "ctx_create: null out");
+  *out = nullptr;
+  meso_config c;
+  memset(&c, 0, sizeof(c));
+  if (cfg) c = *cfg;
+  if ((c.chunk_edge && c.chunk_edge != 32) || (c.brick_edge && c.brick_edge != 8))
+    return fail(MESO_ERR_INVALID_ARG, "ctx_create: chunk edge must be 32 and brick edge 8");
+  int n = 0;
+  MESO_CUDA_TRY(cudaGetDeviceCount(&n));
+  if (c.device < 0 || c.device >= n) return fail(MESO_ERR_INVALID_ARG, "ctx_create: no such device");
+  MESO_CUDA_TRY(cudaSetDevice(c.device));
+  cudaDeviceProp prop;
+  MESO_CUDA_TRY(cudaGetDeviceProperties(&prop, c.device));
+  if (prop.major < 10) return fail(MESO_ERR_CUDA, "ctx_create: needs a Blackwell (sm_10x) device");
+  meso_ctx* ctx = new meso_ctx();
+  ctx->device = c.device;
+  ctx->sm_count = prop.multiProcessorCount;
+  load_tuning(c.tuning_path, ctx->tuning);
+  if (c.mesh_ctas_per_sm) ctx->tuning.mesh_ctas_per_sm = c.mesh_ctas_per_sm;
+  if (c.mesh_chunks_per_ticket) ctx->tuning.mesh_chunks_per_ticket = c.mesh_chunks_per_ticket;
+  if (c.ray_tile_w) ctx->tuning.ray_tile_w = c.ray_tile_w;
+  if (c.ray_warps_per_cta) ctx->tuning.ray_warps_per_cta = c.ray_warps_per_cta;
+  if (32 % ctx->tuning.ray_tile_w || ctx->tuning.ray_warps_per_cta == 0 || ctx->tuning.ray_warps_per_cta > 8) {
+    delete ctx;
+    return fail(MESO_ERR_INVALID_ARG, "ctx_create: bad ray tile configuration");
+  }
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  ctx->budget_bytes = c.hbm_budget_bytes ? c.hbm_budget_bytes : (uint64_t)(free_b * 0.9);
+  cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_scratch, 64);
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_scratch, 0, 64);
+  if (e != cudaSuccess) {
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return cuda_fail(e, "ctx_create");
+  }
+  *out = ctx;
+  return MESO_OK;
+}
+
+void meso_ctx_destroy(meso_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(ctx->d_scratch);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+meso_status meso_sync(meso_ctx* ctx, void* stream) {
+  if (!ctx) return fail(MESO_ERR_INVALID_ARG, "sync: null ctx");
+  MESO_CUDA_TRY(cudaStreamSynchronize(pick_stream(ctx, stream)));
+  uint32_t err = 0;
+  MESO_CUDA_TRY(cudaMemcpy(&err, ctx->d_scratch + 1, 4, cudaMemcpyDeviceToHost));
+  if (err) {
+    cudaMemset(ctx->d_scratch + 1, 0, 4);
+    if (err & ERR_TIMEOUT) return fail(MESO_ERR_TIMEOUT, "a device wait timed out");
+    if (err & ERR_POOL_FULL) return fail(MESO_ERR_OOM, "brick pool exhausted during an edit");
+    if (err & ERR_BAD_INPUT) return fail(MESO_ERR_INVALID_ARG, "chunk coordinate outside the source");
+  }
+  return MESO_OK;
+}
+
+uint64_t meso_kernel_launches(const meso_ctx* ctx) { return ctx ? ctx->launches.load() : 0; }
+int meso_sm_count(const meso_ctx* ctx) { return ctx ? ctx->sm_count : 0; }
+
+meso_status meso_dev_alloc(meso_ctx* ctx, size_t bytes, void** d_ptr) {
+  if (!ctx || !d_ptr) return fail(MESO_ERR_INVALID_ARG, "dev_alloc: null argument");
+  MESO_CUDA_TRY(cudaMalloc(d_ptr, bytes ? bytes : 16));
+  return MESO_OK;
+}
+meso_status meso_dev_free(meso_ctx* ctx, void* d_ptr) {
+  (void)ctx;
+  MESO_CUDA_TRY(cudaFree(d_ptr));
+  return MESO_OK;
+}
+meso_status meso_host_alloc_pinned(meso_ctx* ctx, size_t bytes, void** h_ptr) {
+  if (!ctx || !h_ptr) return fail(MESO_ERR_INVALID_ARG, "host_alloc_pinned: null argument");
+  MESO_CUDA_TRY(cudaMallocHost(h_ptr, bytes ? bytes : 16));
+  return MESO_OK;
+}
+meso_status meso_host_free_pinned(meso_ctx* ctx, void* h_ptr) {
+  (void)ctx;
+  MESO_CUDA_TRY(cudaFreeHost(h_ptr));
+  return MESO_OK;
+}
+meso_status meso_memcpy_h2d(meso_ctx* ctx, void* d_dst, const void* h_src, size_t bytes, void* stream) {
+  MESO_CUDA_TRY(cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, pick_stream(ctx, stream)));
+  return MESO_OK;
+}
+meso_status meso_memcpy_d2h(meso_ctx* ctx, void* h_dst, const void* d_src, size_t bytes, void* stream) {
+  MESO_CUDA_TRY(cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, pick_stream(ctx, stream)));
+  return MESO_OK;
+}
+meso_status meso_memset(meso_ctx* ctx, void* d_dst, int value, size_t bytes, void* stream) {
+  MESO_CUDA_TRY(cudaMemsetAsync(d_dst, value, bytes, pick_stream(ctx, stream)));
+  return MESO_OK;
+}
+meso_status meso_stream_create(meso_ctx* ctx, void** stream) {
+  (void)ctx;
+  cudaStream_t s;
+  MESO_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  *stream = s;
+  return MESO_OK;
+}
+meso_status meso_stream_destroy(meso_ctx* ctx, void* stream) {
+  (void)ctx;
+  MESO_CUDA_TRY(cudaStreamDestroy((cudaStream_t)stream));
+  return MESO_OK;
+}
+meso_status meso_event_create(meso_ctx* ctx, void** ev) {
+  (void)ctx;
+  cudaEvent_t e;
+  MESO_CUDA_TRY(cudaEventCreate(&e));
+  *ev = e;
+  return MESO_OK;
+}
+meso_status meso_event_destroy(meso_ctx* ctx, void* ev) {
+  (void)ctx;
+  MESO_CUDA_TRY(cudaEventDestroy((cudaEvent_t)ev));
+  return MESO_OK;
+}
+meso_status meso_event_record(meso_ctx* ctx, void* ev, void* stream) {
+  MESO_CUDA_TRY(cudaEventRecord((cudaEvent_t)ev, pick_stream(ctx, stream)));
+  return MESO_OK;
+}
+meso_status meso_event_elapsed_ms(meso_ctx* ctx, void* a, void* b, float* ms) {
+  (void)ctx;
+  MESO_CUDA_TRY(cudaEventSynchronize((cudaEvent_t)b));
+  MESO_CUDA_TRY(cudaEventElapsedTime(ms, (cudaEvent_t)a, (cudaEvent_t)b));
+  return MESO_OK;
+}
+
+// ---------------------------------------------------------------- scenes
+
+meso_status meso_scene_create_terrain(meso_ctx* ctx, const meso_terrain* t, uint64_t spare, meso_scene** out) {
+  if (!ctx) return fail(MESO_ERR_INVALID_ARG, "null ctx");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  return scene_create_terrain(ctx, t, spare, out);
+}
+
+meso_status meso_scene_create_dense(meso_ctx* ctx, const uint16_t* h_grid, int32_t nx, int32_t ny, int32_t nz,
+                                    uint64_t spare, meso_scene** out) {
+  if (!ctx) return fail(MESO_ERR_INVALID_ARG, "null ctx");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  return scene_create_dense(ctx, h_grid, nx, ny, nz, spare, out);
+}
+
+meso_status meso_scene_destroy(meso_ctx* ctx, meso_scene* scene) {
+  if (!ctx) return fail(MESO_ERR_INVALID_ARG, "null ctx");
+  cudaDeviceSynchronize();
+  scene_release(ctx, scene);
+  return MESO_OK;
+}
+
+meso_status meso_scene_get_info(meso_ctx* ctx, const meso_scene* s, meso_scene_info* info) {
+  if (!ctx || !s || !info) return fail(MESO_ERR_INVALID_ARG, "scene_get_info: null argument");
+  int32_t alloc[2] = {0, 0};
+  MESO_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  MESO_CUDA_TRY(cudaMemcpy(alloc, s->d_alloc, 8, cudaMemcpyDeviceToHost));
+  info->nx = s->nx;
+  info->ny = s->ny;
+  info->nz = s->nz;
+  info->n_bricks = (uint64_t)(alloc[0] - alloc[1]);
+  info->brick_capacity = s->capacity;
+  info->device_bytes = s->bytes;
+  info->d_ptr = s->d_ptr;
+  info->d_occ = s->d_occ;
+  info->d_mat = s->d_mat;
+  return MESO_OK;
+}
+
+meso_status meso_scene_download(meso_ctx* ctx, const meso_scene* s, uint32_t* h_ptr, uint64_t* h_occ,
+                                uint16_t* h_mat) {
+  if (!ctx || !s) return fail(MESO_ERR_INVALID_ARG, "scene_download: null argument");
+  MESO_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (h_ptr) MESO_CUDA_TRY(cudaMemcpy(h_ptr, s->d_ptr, n_bricks_of(s) * 4, cudaMemcpyDeviceToHost));
+  if (h_occ) MESO_CUDA_TRY(cudaMemcpy(h_occ, s->d_occ, s->capacity * 64, cudaMemcpyDeviceToHost));
+  if (h_mat) MESO_CUDA_TRY(cudaMemcpy(h_mat, s->d_mat, s->capacity * 1024, cudaMemcpyDeviceToHost));
+  return MESO_OK;
+}
+
+meso_status meso_generate_dense_u8(meso_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, uint32_t seed, uint8_t* d_out,
+                                   void* stream) {
+  if (!ctx) return fail(MESO_ERR_INVALID_ARG, "null ctx");
+  return generate_dense_u8(ctx, nx, ny, nz, seed, d_out, pick_stream(ctx, stream));
+}
+
+meso_status meso_generate_chunks_u16(meso_ctx* ctx, uint32_t n, uint32_t seed0, uint16_t* d_out, uint32_t* d_solid,
+                                     void* stream) {
+  if (!ctx) return fail(MESO_ERR_INVALID_ARG, "null ctx");
+  return generate_chunks_u16(ctx, n, seed0, d_out, d_solid, pick_stream(ctx, stream));
+}
+
+// ---------------------------------------------------------------- meshing
+
+meso_status meso_mesh_chunks(meso_ctx* ctx, const meso_mesh_source* src, const int32_t* d_coords, uint32_t n,
+                             const meso_mesh_output* out, void* stream) {
+  if (!ctx) return fail(MESO_ERR_INVALID_ARG, "null ctx");
+  return launch_mesh(ctx, src, d_coords, n, out, pick_stream(ctx, stream), false);
+}
+
+meso_status meso_mesh_chunks_per_launch(meso_ctx* ctx, const meso_mesh_source* src, const int32_t* d_coords,
+                                        uint32_t n, const meso_mesh_output* out, void* stream) {
+  if (!ctx) return fail(MESO_ERR_INVALID_ARG, "null ctx");
+  return launch_mesh(ctx, src, d_coords, n, out, pick_stream(ctx, stream), true);
+}
+
+meso_status meso_mesh_check(meso_ctx* ctx, const meso_mesh_output* out, void* stream, uint64_t* h_count) {
+  if (!ctx || !out) return fail(MESO_ERR_INVALID_ARG, "mesh_check: null argument");
+  cudaStream_t st = pick_stream(ctx, stream);
+  uint64_t cnt = 0;
+  MESO_CUDA_TRY(cudaMemcpyAsync(&cnt, out->d_quad_count, 8, cudaMemcpyDeviceToHost, st));
+  MESO_TRY(meso_sync(ctx, st));
+  if (h_count) *h_count = cnt;
+  if (cnt > out->capacity) return fail(MESO_ERR_OVERFLOW, "mesh: quad buffer too small");
+  return MESO_OK;
+}
+
+meso_status meso_mesh_host(meso_ctx* ctx, int32_t kind, const void* h_data, int32_t nx, int32_t ny, int32_t nz,
+                           const int32_t* h_coords, uint32_t n, uint64_t* h_quads, uint64_t capacity,
+                           uint64_t* h_count) {
+  if (!ctx || !h_data) return fail(MESO_ERR_INVALID_ARG, "mesh_host: null argument");
+  size_t data_bytes;
+  size_t coord_bytes = 0;
+  switch (kind) {
+    case MESO_SRC_CHUNKS_U16:
+      if (nx <= 0) nx = (int32_t)n;
+      data_bytes = (size_t)nx * 65536;
+      coord_bytes = h_coords ? 4ull * n : 0;
+      break;
+    case MESO_SRC_CHUNKS_U8:
+      if (nx <= 0) nx = (int32_t)n;
+      data_bytes = (size_t)nx * 32768;
+      coord_bytes = h_coords ? 4ull * n : 0;
+      break;
+    case MESO_SRC_GRID_U8: data_bytes = (size_t)nx * ny * nz; coord_bytes = 12ull * n; break;
+    case MESO_SRC_GRID_U16: data_bytes = (size_t)nx * ny * nz * 2; coord_bytes = 12ull * n; break;
+    default: return fail(MESO_ERR_INVALID_ARG, "mesh_host: brick-map sources are device-resident; use meso_mesh_chunks");
+  }
+  if (coord_bytes && !h_coords) return fail(MESO_ERR_INVALID_ARG, "mesh_host: grid source needs coordinates");
+  cudaStream_t st = ctx->stream;
+  uint8_t* d = nullptr;
+  const size_t off_coords = (data_bytes + 255) & ~size_t(255);
+  const size_t off_count = (off_coords + coord_bytes + 255) & ~size_t(255);
+  const size_t off_quads = off_count + 256;
+  const size_t total = off_quads + capacity * 8;
+  MESO_CUDA_TRY(cudaMallocAsync(&d, total, st));
+  meso_status rc = MESO_OK;
+  cudaError_t e = cudaMemcpyAsync(d, h_data, data_bytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && coord_bytes) e = cudaMemcpyAsync(d + off_coords, h_coords, coord_bytes, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) rc = cuda_fail(e, "mesh_host upload");
+  meso_mesh_source src;
+  memset(&src, 0, sizeof(src));
+  src.kind = kind;
+  src.d_data = d;
+  src.nx = nx;
+  src.ny = ny;
+  src.nz = nz;
+  meso_mesh_output o;
+  o.d_quads = reinterpret_cast<uint64_t*>(d + off_quads);
+  o.capacity = capacity;
+  o.d_quad_count = reinterpret_cast<uint64_t*>(d + off_count);
+  o.d_chunk_quad_counts = nullptr;
+  if (rc == MESO_OK)
+    rc = launch_mesh(ctx, &src, coord_bytes ? reinterpret_cast<const int32_t*>(d + off_coords) : nullptr, n, &o, st,
+                     false);
+  uint64_t cnt = 0;
+  if (rc == MESO_OK) {
+    e = cudaMemcpyAsync(&cnt, o.d_quad_count, 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "mesh_host");
+  }
+  if (rc == MESO_OK && h_quads && capacity) {
+    const uint64_t k = cnt < capacity ? cnt : capacity;
+    e = cudaMemcpyAsync(h_quads, o.d_quads, k * 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "mesh_host download");
+  }
+  cudaFreeAsync(d, st);
+  if (rc == MESO_OK) rc = meso_sync(ctx, st);
+  if (h_count) *h_count = cnt;
+  if (rc == MESO_OK && cnt > capacity) rc = fail(MESO_ERR_OVERFLOW, "mesh_host: quad buffer too small");
+  return rc;
+}
+
+// -------------------------------------------------------------- raymarching
+
+meso_status meso_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* cams, uint32_t n_views,
+                          const float light[3], uint32_t flags, meso_hit* d_hits, void* stream) {
+  if (!ctx) return fail(MESO_ERR_INVALID_ARG, "null ctx");
+  cudaStream_t st = pick_stream(ctx, stream);
+  if (n_views <= 32) return launch_raymarch(ctx, scenes, cams, n_views, light, flags, d_hits, st, nullptr, 0);
+  const size_t tb = raymarch_view_table_bytes(n_views);
+  void* d_table = nullptr;
+  MESO_CUDA_TRY(cudaMallocAsync(&d_table, tb, st));
+  meso_status rc = launch_raymarch(ctx, scenes, cams, n_views, light, flags, d_hits, st, d_table, tb);
+  cudaFreeAsync(d_table, st);
+  return rc;
+}
+
+meso_status meso_raymarch_per_view(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* cams,
+                                   uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
+                                   void* stream) {
+  if (!ctx || !cams) return fail(MESO_ERR_INVALID_ARG, "raymarch_per_view: null argument");
+  cudaStream_t st = pick_stream(ctx, stream);
+  uint64_t off = 0;
+  for (uint32_t v = 0; v < n_views; v++) {
+    MESO_TRY(launch_raymarch(ctx, scenes + v, cams + v, 1, light, flags, d_hits + off, st, nullptr, 0));
+    off += (uint64_t)cams[v].width * cams[v].height;
+  }
+  return MESO_OK;
+}
+
+meso_status meso_raymarch_host(meso_ctx* ctx, const meso_scene* scene, const meso_camera* cam, const float light[3],
+                               uint32_t flags, meso_hit* h_hits) {
+  if (!ctx || !scene || !cam || !h_hits) return fail(MESO_ERR_INVALID_ARG, "raymarch_host: null argument");
+  cudaStream_t st = ctx->stream;
+  const size_t n = (size_t)cam->width * cam->height;
+  meso_hit* d = nullptr;
+  MESO_CUDA_TRY(cudaMallocAsync(&d, n * sizeof(meso_hit), st));
+  meso_status rc = launch_raymarch(ctx, &scene, cam, 1, light, flags, d, st, nullptr, 0);
+  if (rc == MESO_OK) {
+    cudaError_t e = cudaMemcpyAsync(h_hits, d, n * sizeof(meso_hit), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "raymarch_host");
+  }
+  cudaFreeAsync(d, st);
+  return rc;
+}
+
+// ------------------------------------------------------------------- edits
+
+meso_status meso_edit_spheres(meso_ctx* ctx, meso_scene* scene, const meso_sphere_edit* h_spheres, uint32_t n,
+                              uint32_t* h_dirty, uint32_t dirty_cap, uint32_t* n_dirty, void* stream) {
+  if (!ctx) return fail(MESO_ERR_INVALID_ARG, "null ctx");
+  return edit_spheres(ctx, scene, h_spheres, n, h_dirty, dirty_cap, n_dirty, pick_stream(ctx, stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,601 @@
+// mesh.cu -- greedy chunk meshing on sm_103a.
+//
+// Replaces the reference's per-chunk host work: the 26-neighbour erosion cull
+// (Runtimes/Voxel/Occupancy/BinaryOccupancyVolume.h:76-99, run from
+// Runtimes/Voxel/Chunk/Chunk.h:73-100) and the one-instance-per-visible-block
+// emission of FChunkPool::PushToBlockPool (Runtimes/Voxel/Chunk/ChunkPool.h:381-445),
+// dispatched 8 chunks per host task by FChunkManage::MultiThreadGeneratorBatched
+// (Runtimes/Voxel/Chunk/ChunkManager.h:183-210).  Here a persistent kernel
+// pulls chunks from a device ticket queue and emits greedy quads.
+//
+// Per chunk (one CTA, 8 warps):
+//  1. staging: the 32^3 materials arrive in shared memory through TMA (one
+//     bulk copy per chunk of a chunk array, one 3-D tensor box per chunk of a
+//     dense grid, one 1 KiB bulk copy per occupied brick of a brick map),
+//     double-buffered so the next chunk streams in while this one is meshed;
+//     the one-voxel occupancy halo is read with plain loads meanwhile;
+//  2. masks: lanes = x; every row (y,z) becomes bit-packed words with warp
+//     ballots: occupancy, material-equality with the -x, -y and -z neighbour,
+//     and (accumulated per lane over y) the transposed columns for the X
+//     faces; face masks are occ & ~shift(occ) per direction;
+//  3. greedy: warp = face direction, lane = slice; rows are scanned with
+//     ffs / run-length bit tricks (Lysenko's order: first unconsumed face,
+//     widen along u while the material matches, grow along v while the whole
+//     run matches); quads are staged per warp in shared memory and appended
+//     to global memory with one atomic per ~480 quads.
+#include <cudaTypedefs.h>
+
+#include <cstdio>
+#include <cstring>
+
+#include "meso_internal.h"
+
+namespace meso {
+namespace {
+
+using namespace ::meso::dev;
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kGreedyWarps = 6;
+constexpr int kS = 33;               // padded row stride of 32x32 word arrays
+constexpr int kArr = 32 * kS;
+constexpr int kQBuf = 512;           // staged quads per greedy warp
+constexpr int kBrickSlot = 1040;     // bytes per staged brick (bank-spread padding)
+constexpr int kMatBuf = 64 * kBrickSlot;
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+
+struct __align__(128) MeshSmem {
+  uint8_t mat[2][kMatBuf];
+  uint32_t occ[kArr];
+  uint32_t ex[kArr], ey[kArr], ez[kArr];  // equality with -x / -y / -z neighbour, bits over x, [z][y]
+  uint32_t eyt[kArr], ezt[kArr];          // equality with -y / -z neighbour, bits over y, [z][x]
+  uint32_t f[6][kArr];                    // face masks; X: [z][x] bits y; Y,Z: [z][y] bits x
+  uint32_t halo[6][32];                   // -X,+X: bits y by z; -Y,+Y: bits x by z; -Z,+Z: bits x by y
+  uint64_t qbuf[kGreedyWarps][kQBuf];
+  uint64_t bar[2];
+  int32_t chunk[2];
+  int32_t valid[2];
+  int32_t coord[2][3];
+  uint32_t chunk_quads;
+};
+
+struct MeshParams {
+  const uint8_t* data;
+  int32_t nx, ny, nz;
+  const uint32_t* bptr;
+  const uint64_t* bocc;
+  const uint16_t* bmat;
+  int32_t bx, by, bz;
+  const int32_t* coords;
+  uint32_t n_chunks;
+  uint32_t chunk_id_base;
+  uint64_t* quads;
+  uint64_t cap;
+  unsigned long long* count;
+  uint32_t* chunk_counts;
+  uint32_t* ticket;
+  uint32_t* err;
+  uint32_t per_ticket;
+  int32_t use_queue;
+};
+
+template <int KIND>
+struct KindTraits;
+template <>
+struct KindTraits<MESO_SRC_CHUNKS_U16> {
+  static constexpr bool kHalo = false, kGrid = false, kBrick = false;
+  static constexpr int kElem = 2;
+};
+template <>
+struct KindTraits<MESO_SRC_CHUNKS_U8> {
+  static constexpr bool kHalo = false, kGrid = false, kBrick = false;
+  static constexpr int kElem = 1;
+};
+template <>
+struct KindTraits<MESO_SRC_GRID_U8> {
+  static constexpr bool kHalo = true, kGrid = true, kBrick = false;
+  static constexpr int kElem = 1;
+};
+template <>
+struct KindTraits<MESO_SRC_GRID_U16> {
+  static constexpr bool kHalo = true, kGrid = true, kBrick = false;
+  static constexpr int kElem = 2;
+};
+template <>
+struct KindTraits<MESO_SRC_BRICKMAP> {
+  static constexpr bool kHalo = true, kGrid = false, kBrick = true;
+  static constexpr int kElem = 2;
+};
+
+template <int KIND>
+__device__ __forceinline__ uint32_t load_mat(const uint8_t* buf, int x, int y, int z) {
+  using T = KindTraits<KIND>;
+  if constexpr (T::kBrick) {
+    const int b = (x >> 3) + 4 * (y >> 3) + 16 * (z >> 3);
+    return reinterpret_cast<const uint16_t*>(buf + b * kBrickSlot)[(x & 7) + 8 * (y & 7) + 64 * (z & 7)];
+  } else if constexpr (T::kElem == 2) {
+    return reinterpret_cast<const uint16_t*>(buf)[(z * 32 + y) * 32 + x];
+  } else {
+    return buf[(z * 32 + y) * 32 + x];
+  }
+}
+
+// Occupancy (material != 0) of a global voxel for halo reads; 0 outside.
+template <int KIND>
+__device__ __forceinline__ uint32_t global_solid(const MeshParams& p, int gx, int gy, int gz) {
+  using T = KindTraits<KIND>;
+  if (gx < 0 || gy < 0 || gz < 0) return 0;
+  if constexpr (T::kBrick) {
+    if (gx >= p.bx * 8 || gy >= p.by * 8 || gz >= p.bz * 8) return 0;
+    const uint32_t ptr = __ldg(p.bptr + (gx >> 3) + (size_t)p.bx * ((gy >> 3) + (size_t)p.by * (gz >> 3)));
+    if (ptr == MESO_EMPTY_BRICK) return 0;
+    const uint64_t w = __ldg(p.bocc + (size_t)ptr * 8 + (gz & 7));
+    return (uint32_t)(w >> ((gx & 7) + 8 * (gy & 7))) & 1u;
+  } else {
+    if (gx >= p.nx || gy >= p.ny || gz >= p.nz) return 0;
+    const size_t i = (size_t)gx + (size_t)p.nx * ((size_t)gy + (size_t)p.ny * (size_t)gz);
+    if constexpr (T::kElem == 2) return __ldg(reinterpret_cast<const uint16_t*>(p.data) + i) != 0;
+    else return __ldg(p.data + i) != 0;
+  }
+}
+
+// Producer side: called by warp 0 (all lanes).  Takes the next chunk off the
+// queue and starts its copy into buffer `buf`.
+template <int KIND>
+__device__ __forceinline__ void issue_chunk(MeshSmem& sm, const MeshParams& p, const CUtensorMap* tmap, int buf,
+                                            int lane, uint32_t& cur, uint32_t& end) {
+  using T = KindTraits<KIND>;
+  int c = -1;
+  if (lane == 0) {
+    if (p.use_queue) {
+      if (cur >= end) {
+        cur = atomicAdd(p.ticket, p.per_ticket);
+        end = cur + p.per_ticket;
+      }
+      if (cur < p.n_chunks) c = (int)cur++;
+    } else {
+      if (cur < p.n_chunks) {
+        c = (int)cur;
+        cur += gridDim.x;
+      }
+    }
+  }
+  c = __shfl_sync(kFull, c, 0);
+  if (lane == 0) sm.chunk[buf] = c;
+  if (c < 0) return;
+  uint64_t* bar = &sm.bar[buf];
+  uint8_t* dst = sm.mat[buf];
+  if constexpr (!T::kGrid && !T::kBrick) {
+    if (lane == 0) {
+      // with an index list, p.nx is the number of chunks in the array
+      const uint32_t idx = p.coords ? (uint32_t)p.coords[c] : (uint32_t)c;
+      const bool ok = !p.coords || idx < (uint32_t)p.nx;
+      sm.valid[buf] = ok ? 1 : 0;
+      if (!ok) {
+        atomicOr(p.err, ERR_BAD_INPUT);
+        mbar_arrive_expect_tx(bar, 0);
+      } else {
+        const uint32_t bytes = 32768u * T::kElem;
+        const uint8_t* src = p.data + (size_t)idx * bytes;
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(bar, bytes);
+        for (uint32_t off = 0; off < bytes; off += 16384u) bulk_g2s(dst + off, src + off, 16384u, bar);
+      }
+    }
+  } else {
+    int cx = 0, cy = 0, cz = 0;
+    if (lane == 0) {
+      cx = p.coords[3 * c];
+      cy = p.coords[3 * c + 1];
+      cz = p.coords[3 * c + 2];
+    }
+    cx = __shfl_sync(kFull, cx, 0);
+    cy = __shfl_sync(kFull, cy, 0);
+    cz = __shfl_sync(kFull, cz, 0);
+    int lim_x, lim_y, lim_z;
+    if constexpr (T::kBrick) {
+      lim_x = p.bx / 4;
+      lim_y = p.by / 4;
+      lim_z = p.bz / 4;
+    } else {
+      lim_x = p.nx / 32;
+      lim_y = p.ny / 32;
+      lim_z = p.nz / 32;
+    }
+    const bool ok = cx >= 0 && cy >= 0 && cz >= 0 && cx < lim_x && cy < lim_y && cz < lim_z;
+    if (lane == 0) {
+      sm.coord[buf][0] = cx;
+      sm.coord[buf][1] = cy;
+      sm.coord[buf][2] = cz;
+      sm.valid[buf] = ok ? 1 : 0;
+    }
+    if (!ok) {
+      if (lane == 0) {
+        atomicOr(p.err, ERR_BAD_INPUT);
+        mbar_arrive_expect_tx(bar, 0);
+      }
+      return;
+    }
+    if constexpr (T::kGrid) {
+      if (lane == 0) {
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(bar, 32768u * T::kElem);
+        tma_load_3d(dst, tmap, cx * 32, cy * 32, cz * 32, bar);
+      }
+    } else {
+      // 64 bricks, two per lane
+      uint32_t ptrs[2];
+      for (int k = 0; k < 2; k++) {
+        const int b = lane + 32 * k;
+        const int gx = cx * 4 + (b & 3), gy = cy * 4 + ((b >> 2) & 3), gz = cz * 4 + (b >> 4);
+        ptrs[k] = __ldg(p.bptr + gx + (size_t)p.bx * (gy + (size_t)p.by * gz));
+      }
+      const uint32_t n_full = __popc(__ballot_sync(kFull, ptrs[0] != MESO_EMPTY_BRICK)) +
+                              __popc(__ballot_sync(kFull, ptrs[1] != MESO_EMPTY_BRICK));
+      if (lane == 0) {
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(bar, n_full * 1024u);
+      }
+      __syncwarp();
+      for (int k = 0; k < 2; k++) {
+        const int b = lane + 32 * k;
+        uint8_t* d = dst + b * kBrickSlot;
+        if (ptrs[k] != MESO_EMPTY_BRICK) {
+          bulk_g2s(d, p.bmat + (size_t)ptrs[k] * 512, 1024u, bar);
+        } else {
+          uint4* z4 = reinterpret_cast<uint4*>(d);
+          for (int i = 0; i < 64; i++) z4[i] = make_uint4(0, 0, 0, 0);
+        }
+      }
+    }
+  }
+}
+
+template <int KIND>
+__device__ __forceinline__ void compute_halos(MeshSmem& sm, const MeshParams& p, int buf, int warp, int lane) {
+  const int X = sm.coord[buf][0] * 32, Y = sm.coord[buf][1] * 32, Z = sm.coord[buf][2] * 32;
+  for (int wi = warp; wi < 6 * 32; wi += kWarps) {
+    const int f = wi >> 5, k = wi & 31;
+    int gx, gy, gz;
+    switch (f) {
+      case 0: gx = X - 1; gy = Y + lane; gz = Z + k; break;
+      case 1: gx = X + 32; gy = Y + lane; gz = Z + k; break;
+      case 2: gx = X + lane; gy = Y - 1; gz = Z + k; break;
+      case 3: gx = X + lane; gy = Y + 32; gz = Z + k; break;
+      case 4: gx = X + lane; gy = Y + k; gz = Z - 1; break;
+      default: gx = X + lane; gy = Y + k; gz = Z + 32; break;
+    }
+    const uint32_t w = __ballot_sync(kFull, global_solid<KIND>(p, gx, gy, gz) != 0);
+    if (lane == 0) sm.halo[f][k] = w;
+  }
+}
+
+__device__ __forceinline__ void flush_quads(uint64_t* qb, uint32_t& cnt, const MeshParams& p, int lane) {
+  __syncwarp();
+  unsigned long long base = 0;
+  if (lane == 0 && cnt) base = atomicAdd(p.count, (unsigned long long)cnt);
+  base = __shfl_sync(kFull, base, 0);
+  for (uint32_t i = lane; i < cnt; i += 32) {
+    const unsigned long long idx = base + i;
+    if (idx < p.cap) p.quads[idx] = qb[i];
+  }
+  __syncwarp();
+  cnt = 0;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kThreads, 1)
+    mesh_kernel(const MeshParams p, const __grid_constant__ CUtensorMap tmap) {
+  using T = KindTraits<KIND>;
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t base_addr = smem_u32(smem_raw);
+  const uint32_t pad = (128u - (base_addr & 127u)) & 127u;
+  MeshSmem& sm = *reinterpret_cast<MeshSmem*>(smem_raw + pad);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  uint32_t cur = p.use_queue ? 0u : blockIdx.x, end = 0;
+
+  if (tid == 0) {
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
+    sm.chunk_quads = 0;
+    for (int f = 0; f < 6; f++)
+      for (int k = 0; k < 32; k++) sm.halo[f][k] = 0;
+    fence_proxy_async_smem();
+  }
+  __syncthreads();
+  if (warp == 0) issue_chunk<KIND>(sm, p, &tmap, 0, lane, cur, end);
+  __syncthreads();
+
+  uint32_t phase = 0;  // bit b = parity of buffer b
+  uint32_t qcnt = 0;   // staged quads of this warp (greedy warps)
+  int buf = 0;
+  for (;;) {
+    const int c = sm.chunk[buf];
+    if (c < 0) break;
+    if (warp == 0) issue_chunk<KIND>(sm, p, &tmap, buf ^ 1, lane, cur, end);
+    const bool valid = sm.valid[buf] != 0;
+    if constexpr (T::kHalo) {
+      if (valid) compute_halos<KIND>(sm, p, buf, warp, lane);
+    }
+    const bool ok = mbar_wait_bounded(&sm.bar[buf], (phase >> buf) & 1u, kWaitLimitNs);
+    phase ^= 1u << buf;
+    if (__syncthreads_or(!ok)) {
+      // A copy did not land within the limit: flag it, give the copies still
+      // in flight (this buffer and the prefetch) one more bounded wait, leave.
+      if (tid == 0) {
+        atomicOr(p.err, ERR_TIMEOUT);
+        mbar_wait_bounded(&sm.bar[buf], ((phase >> buf) & 1u) ^ 1u, kWaitLimitNs);
+        if (sm.chunk[buf ^ 1] >= 0)
+          mbar_wait_bounded(&sm.bar[buf ^ 1], (phase >> (buf ^ 1)) & 1u, kWaitLimitNs);
+      }
+      __syncthreads();
+      return;
+    }
+    if (valid) {
+      const uint8_t* mb = sm.mat[buf];
+      // ---- pass 1: row masks (lanes = x) ----
+      for (int z = warp; z < 32; z += kWarps) {
+        uint32_t occT = 0, eyT = 0, ezT = 0, prev_m = 0, prev_occ = 0;
+        const uint32_t hym = sm.halo[2][z], hyp = sm.halo[3][z];
+#pragma unroll 4
+        for (int y = 0; y < 32; y++) {
+          const uint32_t m = load_mat<KIND>(mb, lane, y, z);
+          const uint32_t mz = z > 0 ? load_mat<KIND>(mb, lane, y, z - 1) : 0u;
+          const bool solid = m != 0;
+          const uint32_t ml = __shfl_up_sync(kFull, m, 1);
+          const bool bx = m == ml, by = m == prev_m, bz = m == mz;
+          const uint32_t occw = __ballot_sync(kFull, solid);
+          const uint32_t exw = __ballot_sync(kFull, bx);
+          const uint32_t eyw = __ballot_sync(kFull, by);
+          const uint32_t ezw = __ballot_sync(kFull, bz);
+          occT |= (uint32_t)solid << y;
+          eyT |= (uint32_t)by << y;
+          ezT |= (uint32_t)bz << y;
+          const int o = z * kS + y;
+          switch (lane) {
+            case 0: sm.occ[o] = occw; break;
+            case 1: sm.ex[o] = exw; break;
+            case 2: sm.ey[o] = eyw; break;
+            case 3: sm.ez[o] = ezw; break;
+            case 4: sm.f[3][o] = occw & ~(y > 0 ? prev_occ : hym); break;
+            case 5: if (y > 0) sm.f[2][o - 1] = prev_occ & ~occw; break;
+            case 6: if (y == 31) sm.f[2][o] = occw & ~hyp; break;
+            default: break;
+          }
+          prev_m = m;
+          prev_occ = occw;
+        }
+        uint32_t up = __shfl_down_sync(kFull, occT, 1), dn = __shfl_up_sync(kFull, occT, 1);
+        if (lane == 31) up = sm.halo[1][z];
+        if (lane == 0) dn = sm.halo[0][z];
+        const int o = z * kS + lane;
+        sm.f[0][o] = occT & ~up;
+        sm.f[1][o] = occT & ~dn;
+        sm.eyt[o] = eyT;
+        sm.ezt[o] = ezT;
+      }
+      __syncthreads();
+      // ---- pass 2: +Z / -Z face masks ----
+      for (int i = tid; i < 1024; i += kThreads) {
+        const int z = i >> 5, y = i & 31, o = z * kS + y;
+        const uint32_t oc = sm.occ[o];
+        const uint32_t up = z < 31 ? sm.occ[o + kS] : sm.halo[5][y];
+        const uint32_t dn = z > 0 ? sm.occ[o - kS] : sm.halo[4][y];
+        sm.f[4][o] = oc & ~up;
+        sm.f[5][o] = oc & ~dn;
+      }
+      __syncthreads();
+      // ---- pass 3: greedy, warp = direction, lane = slice ----
+      if (warp < kGreedyWarps) {
+        const int dir = warp, s = lane;
+        uint32_t* F = sm.f[dir];
+        const uint32_t* E;
+        const uint32_t* V;
+        int ss, sv;
+        if (dir < 2) {
+          E = sm.eyt; V = sm.ezt; ss = 1; sv = kS;
+        } else if (dir < 4) {
+          E = sm.ex; V = sm.ez; ss = 1; sv = kS;
+        } else {
+          E = sm.ex; V = sm.ey; ss = kS; sv = 1;
+        }
+        const uint64_t chunk_bits = (uint64_t)((p.chunk_id_base + (uint32_t)c) & 0xFFFFFu) << 44 |
+                                    (uint64_t)dir << 41;
+        uint64_t* qb = sm.qbuf[warp];
+        uint32_t mine = 0;
+        for (int v = 0; v < 32; v++) {
+          const int o = s * ss + v * sv;
+          uint32_t m = F[o];
+          const uint32_t e = E[o];
+          for (;;) {
+            if (qcnt > (uint32_t)(kQBuf - 32)) flush_quads(qb, qcnt, p, lane);
+            const bool have = m != 0;
+            const uint32_t act = __ballot_sync(kFull, have);
+            if (!act) break;
+            uint64_t q = 0;
+            if (have) {
+              const int u0 = __ffs(m) - 1;
+              const uint32_t run = (uint32_t)((uint64_t)(m & e) >> (u0 + 1));
+              const int w = __ffs(~run);  // 1..32
+              const uint32_t mask = (w == 32 ? kFull : ((1u << w) - 1u)) << u0;
+              int h = 1;
+              for (int r = v + 1; r < 32; r++) {
+                const int orow = s * ss + r * sv;
+                const uint32_t fr = F[orow];
+                if ((fr & V[orow] & mask) != mask) break;
+                F[orow] = fr & ~mask;
+                h++;
+              }
+              m &= ~mask;
+              int x, y, z;
+              if (dir < 2) { x = s; y = u0; z = v; }
+              else if (dir < 4) { x = u0; y = s; z = v; }
+              else { x = u0; y = v; z = s; }
+              const uint32_t mat = load_mat<KIND>(mb, x, y, z);
+              q = chunk_bits | (uint64_t)z << 36 | (uint64_t)y << 31 | (uint64_t)x << 26 |
+                  (uint64_t)(w - 1) << 21 | (uint64_t)(h - 1) << 16 | (uint64_t)mat;
+              mine++;
+            }
+            const uint32_t rank = __popc(act & lanemask_lt());
+            if (have) qb[qcnt + rank] = q;
+            qcnt += __popc(act);
+          }
+        }
+        if (p.chunk_counts) {
+          const uint32_t tot = __reduce_add_sync(kFull, mine);
+          if (lane == 0) atomicAdd(&sm.chunk_quads, tot);
+        }
+      }
+    }
+    __syncthreads();
+    if (tid == 0 && p.chunk_counts) {
+      p.chunk_counts[c] = valid ? sm.chunk_quads : 0u;
+      sm.chunk_quads = 0;
+    }
+    buf ^= 1;
+  }
+  if (warp < kGreedyWarps) flush_quads(sm.qbuf[warp], qcnt, p, lane);
+}
+
+// --------------------------------------------------------------- host side
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  });
+  return fn;
+}
+
+meso_status make_grid_map(const meso_mesh_source* src, int elem, CUtensorMap* map) {
+  auto enc = get_encode_fn();
+  if (!enc) return fail(MESO_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  cuuint64_t dims[3] = {(cuuint64_t)src->nx, (cuuint64_t)src->ny, (cuuint64_t)src->nz};
+  cuuint64_t strides[2] = {(cuuint64_t)src->nx * elem, (cuuint64_t)src->nx * src->ny * elem};
+  cuuint32_t box[3] = {32, 32, 32};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(map, elem == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_UINT8, 3,
+                   const_cast<void*>(src->d_data), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(MESO_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return MESO_OK;
+}
+
+template <int KIND>
+meso_status launch_kind(meso_ctx* ctx, const MeshParams& base, const CUtensorMap& tmap, uint32_t n_chunks,
+                        cudaStream_t st, bool per_launch) {
+  const size_t smem = sizeof(MeshSmem) + 128;
+  static bool attr_set[64] = {false};
+  if (!attr_set[ctx->device & 63]) {
+    MESO_CUDA_TRY(cudaFuncSetAttribute(mesh_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set[ctx->device & 63] = true;
+  }
+  constexpr bool kCoords3 = KindTraits<KIND>::kGrid || KindTraits<KIND>::kBrick;
+  if (per_launch) {
+    for (uint32_t i = 0; i < n_chunks; i++) {
+      MeshParams p = base;
+      p.n_chunks = 1;
+      p.chunk_id_base = i;
+      p.use_queue = 0;
+      if (kCoords3) p.coords = base.coords + 3 * (size_t)i;
+      else if (base.coords) p.coords = base.coords + i;
+      else p.data = base.data + (size_t)i * 32768u * KindTraits<KIND>::kElem;
+      if (p.chunk_counts) p.chunk_counts = base.chunk_counts + i;
+      mesh_kernel<KIND><<<1, kThreads, smem, st>>>(p, tmap);
+      ctx->launches.fetch_add(1);
+    }
+    MESO_CUDA_TRY(cudaGetLastError());
+    return MESO_OK;
+  }
+  MeshParams p = base;
+  p.use_queue = 1;
+  uint32_t grid = ctx->sm_count * (ctx->tuning.mesh_ctas_per_sm ? ctx->tuning.mesh_ctas_per_sm : 1);
+  const uint32_t per = p.per_ticket ? p.per_ticket : 1;
+  const uint32_t need = (n_chunks + per - 1) / per;
+  if (grid > need) grid = need;
+  if (grid == 0) grid = 1;
+  MESO_CUDA_TRY(cudaMemsetAsync(p.ticket, 0, sizeof(uint32_t), st));
+  mesh_kernel<KIND><<<grid, kThreads, smem, st>>>(p, tmap);
+  ctx->launches.fetch_add(1);
+  MESO_CUDA_TRY(cudaGetLastError());
+  return MESO_OK;
+}
+
+}  // namespace
+
+meso_status launch_mesh(meso_ctx* ctx, const meso_mesh_source* src, const int32_t* d_coords, uint32_t n_chunks,
+                        const meso_mesh_output* out, cudaStream_t st, bool per_launch) {
+  if (!src || !out || !out->d_quad_count) return fail(MESO_ERR_INVALID_ARG, "mesh: null source/output");
+  if (n_chunks > MESO_MAX_CHUNKS_PER_CALL) return fail(MESO_ERR_INVALID_ARG, "mesh: more than 2^20 chunks");
+  if (out->capacity && !out->d_quads) return fail(MESO_ERR_INVALID_ARG, "mesh: capacity without buffer");
+  MeshParams p;
+  memset(&p, 0, sizeof(p));
+  p.coords = d_coords;
+  p.n_chunks = n_chunks;
+  p.quads = out->d_quads;
+  p.cap = out->capacity;
+  p.count = reinterpret_cast<unsigned long long*>(out->d_quad_count);
+  p.chunk_counts = out->d_chunk_quad_counts;
+  p.ticket = ctx->d_scratch + 0;
+  p.err = ctx->d_scratch + 1;
+  p.per_ticket = ctx->tuning.mesh_chunks_per_ticket ? ctx->tuning.mesh_chunks_per_ticket : 1;
+  CUtensorMap tmap;
+  memset(&tmap, 0, sizeof(tmap));
+  const int kind = src->kind;
+  if (kind == MESO_SRC_BRICKMAP) {
+    const meso_scene* s = src->scene;
+    if (!s) return fail(MESO_ERR_INVALID_ARG, "mesh: brick-map source without scene");
+    if (s->nx % 32 || s->ny % 32 || s->nz % 32) return fail(MESO_ERR_INVALID_ARG, "mesh: scene dims not multiples of 32");
+    if (!d_coords && n_chunks) return fail(MESO_ERR_INVALID_ARG, "mesh: brick-map source needs chunk coordinates");
+    p.bptr = s->d_ptr;
+    p.bocc = s->d_occ;
+    p.bmat = s->d_mat;
+    p.bx = s->bx;
+    p.by = s->by;
+    p.bz = s->bz;
+  } else {
+    if (!src->d_data && n_chunks) return fail(MESO_ERR_INVALID_ARG, "mesh: null data");
+    p.data = static_cast<const uint8_t*>(src->d_data);
+    p.nx = src->nx;
+    p.ny = src->ny;
+    p.nz = src->nz;
+    if (kind == MESO_SRC_GRID_U8 || kind == MESO_SRC_GRID_U16) {
+      if (src->nx <= 0 || src->ny <= 0 || src->nz <= 0 || src->nx % 32 || src->ny % 32 || src->nz % 32)
+        return fail(MESO_ERR_INVALID_ARG, "mesh: grid dims must be positive multiples of 32");
+      if (!d_coords && n_chunks) return fail(MESO_ERR_INVALID_ARG, "mesh: grid source needs chunk coordinates");
+      if ((reinterpret_cast<uintptr_t>(src->d_data) & 15u) != 0)
+        return fail(MESO_ERR_INVALID_ARG, "mesh: grid base must be 16-byte aligned");
+      MESO_TRY(make_grid_map(src, kind == MESO_SRC_GRID_U16 ? 2 : 1, &tmap));
+    } else if (kind == MESO_SRC_CHUNKS_U16 || kind == MESO_SRC_CHUNKS_U8) {
+      if ((reinterpret_cast<uintptr_t>(src->d_data) & 15u) != 0)
+        return fail(MESO_ERR_INVALID_ARG, "mesh: chunk array must be 16-byte aligned");
+      if (d_coords && src->nx <= 0)
+        return fail(MESO_ERR_INVALID_ARG, "mesh: an index list needs nx = number of chunks in the array");
+    } else {
+      return fail(MESO_ERR_INVALID_ARG, "mesh: unknown source kind");
+    }
+  }
+  MESO_CUDA_TRY(cudaMemsetAsync(out->d_quad_count, 0, sizeof(uint64_t), st));
+  if (n_chunks == 0) return MESO_OK;
+  switch (kind) {
+    case MESO_SRC_CHUNKS_U16: return launch_kind<MESO_SRC_CHUNKS_U16>(ctx, p, tmap, n_chunks, st, per_launch);
+    case MESO_SRC_CHUNKS_U8: return launch_kind<MESO_SRC_CHUNKS_U8>(ctx, p, tmap, n_chunks, st, per_launch);
+    case MESO_SRC_GRID_U8: return launch_kind<MESO_SRC_GRID_U8>(ctx, p, tmap, n_chunks, st, per_launch);
+    case MESO_SRC_GRID_U16: return launch_kind<MESO_SRC_GRID_U16>(ctx, p, tmap, n_chunks, st, per_launch);
+    default: return launch_kind<MESO_SRC_BRICKMAP>(ctx, p, tmap, n_chunks, st, per_launch);
+  }
+}
+
+size_t mesh_smem_bytes() { return sizeof(MeshSmem) + 128; }
+
+}  // namespace meso

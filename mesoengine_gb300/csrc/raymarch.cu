@@ -1,0 +1,426 @@
+// raymarch.cu -- two-level brick-map DDA with a fused shadow ray, sm_103a.
+//
+// Replaces the reference's render step: an instanced draw of MaxBlockCount
+// 7-vertex imposter cubes whose vertex shader places each visible block
+// relative to the chunk-rebased camera (Samples/SimpleVoxel.cpp:146-192, draw
+// at :383-387).  Here every pixel is one thread; a warp covers a tw x (32/tw)
+// pixel tile so neighbouring rays walk the same bricks; many views (cameras,
+// scenes) share one launch through a per-view descriptor table.
+//
+// Traversal (Amanatides & Woo 1987, at two levels): bricks whose pointer is
+// empty are crossed in one coarse step; inside an occupied brick every voxel
+// advance is a fine step over the brick's 8x8x8 occupancy bits.  Boundary
+// times are recomputed from integer coordinates at every step,
+// t = (b - o) * (1/d), with correctly rounded single operations
+// (__fsub_rn/__fmul_rn...) so the results are bit-identical to a host
+// evaluation of the same sequence.  Equal boundary times break x < y < z.
+#include <cstring>
+
+#include "meso_internal.h"
+
+namespace meso {
+
+struct RayView {
+  const uint32_t* ptr;
+  const uint64_t* occ;
+  const uint16_t* mat;
+  int32_t nx, ny, nz;
+  int32_t cam_chunk[3];
+  float o[3];
+  float fwd[3], right[3], up[3];
+  float tan_half;
+  uint32_t width, height;
+  uint32_t tiles_x;
+  uint32_t tile_start;
+  uint64_t hit_offset;
+};
+
+namespace {
+
+using namespace ::meso::dev;
+
+constexpr int kInlineViews = 32;
+constexpr float kInf = __builtin_huge_valf();
+
+struct InlineViews {
+  RayView v[kInlineViews];
+};
+
+struct RayParams {
+  const RayView* table;  // device table (n_views > kInlineViews) or null
+  uint32_t n_views;
+  uint32_t total_tiles;
+  uint32_t tile_w, tile_h;
+  float light[3];
+  uint32_t shadow;
+  meso_hit* hits;
+};
+
+struct Trav {
+  int hit;
+  int vx, vy, vz;
+  float t;
+  int axis;
+  uint32_t coarse, fine;
+};
+
+__device__ __forceinline__ float bound_time(int b, float o, float inv) {
+  return __fmul_rn(__fsub_rn(__int2float_rn(b), o), inv);
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Walks from voxel (vx,vy,vz) (absolute, inside the grid) at time t, entered
+// through axis ea (-1 none).  Ray coordinates are relative to the absolute
+// voxel (bx0,by0,bz0).
+__device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int bz0, float ox, float oy, float oz,
+                                         float dx, float dy, float dz, int vx, int vy, int vz, float t, int ea,
+                                         Trav& r) {
+  const int sx = dx > 0.0f ? 1 : (dx < 0.0f ? -1 : 0);
+  const int sy = dy > 0.0f ? 1 : (dy < 0.0f ? -1 : 0);
+  const int sz = dz > 0.0f ? 1 : (dz < 0.0f ? -1 : 0);
+  const float ix = sx ? __fdiv_rn(1.0f, dx) : 0.0f;
+  const float iy = sy ? __fdiv_rn(1.0f, dy) : 0.0f;
+  const float iz = sz ? __fdiv_rn(1.0f, dz) : 0.0f;
+  const int px = sx > 0 ? 1 : 0, py = sy > 0 ? 1 : 0, pz = sz > 0 ? 1 : 0;
+  const int NBx = V.nx >> 3, NBy = V.ny >> 3, NBz = V.nz >> 3;
+  int Bx = vx >> 3, By = vy >> 3, Bz = vz >> 3;
+  uint32_t cs = 0, fs = 0;
+  const uint32_t cap = (uint32_t)(4 * (V.nx + V.ny + V.nz) + 64);
+  r.hit = 0;
+  for (;;) {
+    if (cs + fs > cap) break;
+    const uint32_t p = __ldg(V.ptr + (size_t)Bx + (size_t)NBx * ((size_t)By + (size_t)NBy * (size_t)Bz));
+    if (p == MESO_EMPTY_BRICK) {
+      const float tx = sx ? bound_time((Bx + px) * 8 - bx0, ox, ix) : kInf;
+      const float ty = sy ? bound_time((By + py) * 8 - by0, oy, iy) : kInf;
+      const float tz = sz ? bound_time((Bz + pz) * 8 - bz0, oz, iz) : kInf;
+      int a = 0;
+      float tm = tx;
+      if (ty < tm) { a = 1; tm = ty; }
+      if (tz < tm) { a = 2; tm = tz; }
+      cs++;
+      t = tm;
+      ea = a;
+      bool out;
+      if (a == 0) {
+        Bx += sx;
+        out = Bx < 0 || Bx >= NBx;
+        vx = sx > 0 ? Bx * 8 : Bx * 8 + 7;
+        vy = clampi((int)floorf(__fadd_rn(oy, __fmul_rn(dy, t))) + by0, By * 8, By * 8 + 7);
+        vz = clampi((int)floorf(__fadd_rn(oz, __fmul_rn(dz, t))) + bz0, Bz * 8, Bz * 8 + 7);
+      } else if (a == 1) {
+        By += sy;
+        out = By < 0 || By >= NBy;
+        vy = sy > 0 ? By * 8 : By * 8 + 7;
+        vx = clampi((int)floorf(__fadd_rn(ox, __fmul_rn(dx, t))) + bx0, Bx * 8, Bx * 8 + 7);
+        vz = clampi((int)floorf(__fadd_rn(oz, __fmul_rn(dz, t))) + bz0, Bz * 8, Bz * 8 + 7);
+      } else {
+        Bz += sz;
+        out = Bz < 0 || Bz >= NBz;
+        vz = sz > 0 ? Bz * 8 : Bz * 8 + 7;
+        vx = clampi((int)floorf(__fadd_rn(ox, __fmul_rn(dx, t))) + bx0, Bx * 8, Bx * 8 + 7);
+        vy = clampi((int)floorf(__fadd_rn(oy, __fmul_rn(dy, t))) + by0, By * 8, By * 8 + 7);
+      }
+      if (out) break;
+      continue;
+    }
+    const uint64_t* occ = V.occ + (size_t)p * 8;
+    bool left = false;
+    for (;;) {
+      const uint64_t w = __ldg(occ + (vz & 7));
+      if ((w >> ((vx & 7) + 8 * (vy & 7))) & 1ull) {
+        r.hit = 1;
+        break;
+      }
+      const float tx = sx ? bound_time(vx + px - bx0, ox, ix) : kInf;
+      const float ty = sy ? bound_time(vy + py - by0, oy, iy) : kInf;
+      const float tz = sz ? bound_time(vz + pz - bz0, oz, iz) : kInf;
+      int a = 0;
+      float tm = tx;
+      if (ty < tm) { a = 1; tm = ty; }
+      if (tz < tm) { a = 2; tm = tz; }
+      fs++;
+      t = tm;
+      ea = a;
+      bool exit_brick;
+      if (a == 0) {
+        vx += sx;
+        exit_brick = (vx >> 3) != Bx;
+        if (exit_brick) { Bx += sx; left = Bx < 0 || Bx >= NBx; }
+      } else if (a == 1) {
+        vy += sy;
+        exit_brick = (vy >> 3) != By;
+        if (exit_brick) { By += sy; left = By < 0 || By >= NBy; }
+      } else {
+        vz += sz;
+        exit_brick = (vz >> 3) != Bz;
+        if (exit_brick) { Bz += sz; left = Bz < 0 || Bz >= NBz; }
+      }
+      if (exit_brick) break;
+      if (cs + fs > cap) { left = true; break; }
+    }
+    if (r.hit || left) break;
+  }
+  r.vx = vx;
+  r.vy = vy;
+  r.vz = vz;
+  r.t = t;
+  r.axis = ea;
+  r.coarse = cs;
+  r.fine = fs;
+}
+
+__device__ __forceinline__ void camera_ray(const RayView& V, uint32_t px, uint32_t py, float& dx, float& dy,
+                                           float& dz) {
+  const float fw = __uint2float_rn(V.width), fh = __uint2float_rn(V.height);
+  const float aspect = __fdiv_rn(fw, fh);
+  float sxv = __fdiv_rn(__uint2float_rn(2u * px + 1u), fw);
+  sxv = __fsub_rn(sxv, 1.0f);
+  sxv = __fmul_rn(sxv, V.tan_half);
+  sxv = __fmul_rn(sxv, aspect);
+  float syv = __fdiv_rn(__uint2float_rn(2u * py + 1u), fh);
+  syv = __fsub_rn(1.0f, syv);
+  syv = __fmul_rn(syv, V.tan_half);
+  float d0 = __fadd_rn(__fadd_rn(V.fwd[0], __fmul_rn(V.right[0], sxv)), __fmul_rn(V.up[0], syv));
+  float d1 = __fadd_rn(__fadd_rn(V.fwd[1], __fmul_rn(V.right[1], sxv)), __fmul_rn(V.up[1], syv));
+  float d2 = __fadd_rn(__fadd_rn(V.fwd[2], __fmul_rn(V.right[2], sxv)), __fmul_rn(V.up[2], syv));
+  float n2 = __fmul_rn(d0, d0);
+  n2 = __fadd_rn(n2, __fmul_rn(d1, d1));
+  n2 = __fadd_rn(n2, __fmul_rn(d2, d2));
+  const float len = __fsqrt_rn(n2);
+  dx = __fdiv_rn(d0, len);
+  dy = __fdiv_rn(d1, len);
+  dz = __fdiv_rn(d2, len);
+}
+
+__device__ __forceinline__ void trace_pixel(const RayView& V, uint32_t px, uint32_t py, const RayParams& P,
+                                            meso_hit& h) {
+  h.voxel = ~0ull;
+  h.t = kInf;
+  h.material = 0;
+  h.face = 6;
+  h.shadow = 255;
+  h.steps = 0;
+  h.shadow_steps = 0;
+  float dx, dy, dz;
+  camera_ray(V, px, py, dx, dy, dz);
+  const int bx0 = V.cam_chunk[0] * 32, by0 = V.cam_chunk[1] * 32, bz0 = V.cam_chunk[2] * 32;
+  const float ox = V.o[0], oy = V.o[1], oz = V.o[2];
+  const int sx = dx > 0.0f ? 1 : (dx < 0.0f ? -1 : 0);
+  const int sy = dy > 0.0f ? 1 : (dy < 0.0f ? -1 : 0);
+  const int sz = dz > 0.0f ? 1 : (dz < 0.0f ? -1 : 0);
+  // slab test against [-base, N - base)
+  float tnear = -kInf, tfar = kInf;
+  int ea = -1;
+  {
+    const float lo = __int2float_rn(-bx0), hi = __int2float_rn(V.nx - bx0);
+    if (!sx) {
+      if (ox < lo || ox >= hi) return;
+    } else {
+      const float inv = __fdiv_rn(1.0f, dx);
+      const float t1 = __fmul_rn(__fsub_rn(lo, ox), inv), t2 = __fmul_rn(__fsub_rn(hi, ox), inv);
+      const float tn = sx > 0 ? t1 : t2, tf = sx > 0 ? t2 : t1;
+      if (tn > tnear) { tnear = tn; ea = 0; }
+      if (tf < tfar) tfar = tf;
+    }
+  }
+  {
+    const float lo = __int2float_rn(-by0), hi = __int2float_rn(V.ny - by0);
+    if (!sy) {
+      if (oy < lo || oy >= hi) return;
+    } else {
+      const float inv = __fdiv_rn(1.0f, dy);
+      const float t1 = __fmul_rn(__fsub_rn(lo, oy), inv), t2 = __fmul_rn(__fsub_rn(hi, oy), inv);
+      const float tn = sy > 0 ? t1 : t2, tf = sy > 0 ? t2 : t1;
+      if (tn > tnear) { tnear = tn; ea = 1; }
+      if (tf < tfar) tfar = tf;
+    }
+  }
+  {
+    const float lo = __int2float_rn(-bz0), hi = __int2float_rn(V.nz - bz0);
+    if (!sz) {
+      if (oz < lo || oz >= hi) return;
+    } else {
+      const float inv = __fdiv_rn(1.0f, dz);
+      const float t1 = __fmul_rn(__fsub_rn(lo, oz), inv), t2 = __fmul_rn(__fsub_rn(hi, oz), inv);
+      const float tn = sz > 0 ? t1 : t2, tf = sz > 0 ? t2 : t1;
+      if (tn > tnear) { tnear = tn; ea = 2; }
+      if (tf < tfar) tfar = tf;
+    }
+  }
+  if (!(tnear < tfar) || !(tfar > 0.0f)) return;
+  int vx, vy, vz;
+  float t0;
+  if (tnear > 0.0f) {
+    t0 = tnear;
+    vx = ea == 0 ? (sx > 0 ? 0 : V.nx - 1)
+                 : clampi((int)floorf(__fadd_rn(ox, __fmul_rn(dx, t0))) + bx0, 0, V.nx - 1);
+    vy = ea == 1 ? (sy > 0 ? 0 : V.ny - 1)
+                 : clampi((int)floorf(__fadd_rn(oy, __fmul_rn(dy, t0))) + by0, 0, V.ny - 1);
+    vz = ea == 2 ? (sz > 0 ? 0 : V.nz - 1)
+                 : clampi((int)floorf(__fadd_rn(oz, __fmul_rn(dz, t0))) + bz0, 0, V.nz - 1);
+  } else {
+    t0 = 0.0f;
+    ea = -1;
+    vx = clampi((int)floorf(ox) + bx0, 0, V.nx - 1);
+    vy = clampi((int)floorf(oy) + by0, 0, V.ny - 1);
+    vz = clampi((int)floorf(oz) + bz0, 0, V.nz - 1);
+  }
+  Trav r;
+  traverse(V, bx0, by0, bz0, ox, oy, oz, dx, dy, dz, vx, vy, vz, t0, ea, r);
+  h.steps = r.fine | (r.coarse << 16);
+  if (!r.hit) return;
+  h.voxel = (uint64_t)r.vx + (uint64_t)V.nx * ((uint64_t)r.vy + (uint64_t)V.ny * (uint64_t)r.vz);
+  h.t = r.t;
+  {
+    const uint32_t p =
+        __ldg(V.ptr + (size_t)(r.vx >> 3) + (size_t)(V.nx >> 3) * ((size_t)(r.vy >> 3) + (size_t)(V.ny >> 3) * (r.vz >> 3)));
+    h.material = __ldg(V.mat + (size_t)p * 512 + (r.vx & 7) + 8 * (r.vy & 7) + 64 * (r.vz & 7));
+  }
+  if (r.axis < 0) return;
+  const int sa = r.axis == 0 ? sx : (r.axis == 1 ? sy : sz);
+  h.face = (uint8_t)(2 * r.axis + (sa > 0 ? 1 : 0));
+  if (!P.shadow) return;
+  int Sx = r.vx, Sy = r.vy, Sz = r.vz;
+  bool outside;
+  if (r.axis == 0) { Sx -= sx; outside = Sx < 0 || Sx >= V.nx; }
+  else if (r.axis == 1) { Sy -= sy; outside = Sy < 0 || Sy >= V.ny; }
+  else { Sz -= sz; outside = Sz < 0 || Sz >= V.nz; }
+  if (outside) {
+    h.shadow = 0;
+    return;
+  }
+  Trav sr;
+  traverse(V, Sx, Sy, Sz, 0.5f, 0.5f, 0.5f, P.light[0], P.light[1], P.light[2], Sx, Sy, Sz, 0.0f, -1, sr);
+  h.shadow = (uint8_t)(sr.hit ? 1 : 0);
+  h.shadow_steps = sr.fine | (sr.coarse << 16);
+}
+
+__device__ __forceinline__ void store_hit(meso_hit* dst, const meso_hit& h) {
+  uint64_t* d = reinterpret_cast<uint64_t*>(dst);
+  const uint64_t w1 = (uint64_t)__float_as_uint(h.t) | (uint64_t)h.material << 32 | (uint64_t)h.face << 48 |
+                      (uint64_t)h.shadow << 56;
+  const uint64_t w2 = (uint64_t)h.steps | (uint64_t)h.shadow_steps << 32;
+  d[0] = h.voxel;
+  d[1] = w1;
+  d[2] = w2;
+}
+
+template <bool kInline>
+__global__ void __launch_bounds__(256) raymarch_kernel(const RayParams P, const __grid_constant__ InlineViews iv) {
+  const uint32_t warps = blockDim.x >> 5;
+  const uint32_t tile = blockIdx.x * warps + (threadIdx.x >> 5);
+  if (tile >= P.total_tiles) return;
+  const int lane = threadIdx.x & 31;
+  const RayView* views = kInline ? iv.v : P.table;
+  // view lookup: last view whose tile_start <= tile
+  uint32_t lo = 0, hi = P.n_views;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (views[mid].tile_start <= tile) lo = mid;
+    else hi = mid;
+  }
+  const RayView& V = views[lo];
+  const uint32_t lt = tile - V.tile_start;
+  const uint32_t tx = lt % V.tiles_x, ty = lt / V.tiles_x;
+  const uint32_t px = tx * P.tile_w + (uint32_t)lane % P.tile_w;
+  const uint32_t py = ty * P.tile_h + (uint32_t)lane / P.tile_w;
+  if (px >= V.width || py >= V.height) return;
+  meso_hit h;
+  trace_pixel(V, px, py, P, h);
+  store_hit(P.hits + V.hit_offset + (uint64_t)py * V.width + px, h);
+}
+
+}  // namespace
+
+size_t raymarch_view_table_bytes(uint32_t n_views) { return sizeof(RayView) * (size_t)n_views; }
+
+// Fills view descriptors (host) for n_views cameras; returns total tiles.
+static uint64_t fill_views(const meso_scene* const* scenes, const meso_camera* cams, uint32_t n_views, uint32_t tw,
+                           uint32_t th, RayView* out) {
+  uint64_t tiles = 0, hits = 0;
+  for (uint32_t v = 0; v < n_views; v++) {
+    const meso_scene* s = scenes[v];
+    const meso_camera& c = cams[v];
+    RayView& V = out[v];
+    memset(&V, 0, sizeof(V));
+    V.ptr = s->d_ptr;
+    V.occ = s->d_occ;
+    V.mat = s->d_mat;
+    V.nx = s->nx;
+    V.ny = s->ny;
+    V.nz = s->nz;
+    for (int a = 0; a < 3; a++) {
+      V.cam_chunk[a] = c.origin_chunk[a];
+      V.o[a] = c.origin_frac[a];
+      V.fwd[a] = c.forward[a];
+      V.right[a] = c.right[a];
+      V.up[a] = c.up[a];
+    }
+    V.tan_half = c.tan_half_fov_y;
+    V.width = c.width;
+    V.height = c.height;
+    V.tiles_x = (c.width + tw - 1) / tw;
+    const uint32_t tiles_y = (c.height + th - 1) / th;
+    V.tile_start = (uint32_t)tiles;
+    V.hit_offset = hits;
+    tiles += (uint64_t)V.tiles_x * tiles_y;
+    hits += (uint64_t)c.width * c.height;
+  }
+  return tiles;
+}
+
+meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* cams,
+                            uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
+                            cudaStream_t st, void* d_view_table, size_t view_table_bytes) {
+  if (!scenes || !cams || !d_hits) return fail(MESO_ERR_INVALID_ARG, "raymarch: null argument");
+  if (n_views == 0) return MESO_OK;
+  for (uint32_t v = 0; v < n_views; v++) {
+    if (!scenes[v]) return fail(MESO_ERR_INVALID_ARG, "raymarch: null scene");
+    if (cams[v].width == 0 || cams[v].height == 0 || cams[v].width > 16384 || cams[v].height > 16384)
+      return fail(MESO_ERR_INVALID_ARG, "raymarch: image size out of range");
+  }
+  if ((flags & MESO_RAY_SHADOW) && !light) return fail(MESO_ERR_INVALID_ARG, "raymarch: shadow without light");
+  const uint32_t tw = ctx->tuning.ray_tile_w ? ctx->tuning.ray_tile_w : 8;
+  if (32 % tw) return fail(MESO_ERR_INVALID_ARG, "raymarch: tile width must divide 32");
+  const uint32_t th = 32 / tw;
+  const uint32_t wpc = ctx->tuning.ray_warps_per_cta ? ctx->tuning.ray_warps_per_cta : 4;
+  RayParams P;
+  memset(&P, 0, sizeof(P));
+  P.n_views = n_views;
+  P.tile_w = tw;
+  P.tile_h = th;
+  P.shadow = (flags & MESO_RAY_SHADOW) ? 1u : 0u;
+  if (light)
+    for (int a = 0; a < 3; a++) P.light[a] = light[a];
+  P.hits = d_hits;
+  static InlineViews empty_views;  // zero-initialised
+  uint64_t tiles;
+  if (n_views <= (uint32_t)kInlineViews) {
+    InlineViews iv;
+    tiles = fill_views(scenes, cams, n_views, tw, th, iv.v);
+    if (tiles >= (1ull << 31)) return fail(MESO_ERR_INVALID_ARG, "raymarch: too many tiles");
+    P.total_tiles = (uint32_t)tiles;
+    const uint32_t blocks = (uint32_t)((tiles + wpc - 1) / wpc);
+    raymarch_kernel<true><<<blocks, wpc * 32, 0, st>>>(P, iv);
+  } else {
+    if (!d_view_table || view_table_bytes < raymarch_view_table_bytes(n_views))
+      return fail(MESO_ERR_INVALID_ARG, "raymarch: view table too small");
+    std::vector<RayView> host(n_views);
+    tiles = fill_views(scenes, cams, n_views, tw, th, host.data());
+    if (tiles >= (1ull << 31)) return fail(MESO_ERR_INVALID_ARG, "raymarch: too many tiles");
+    P.total_tiles = (uint32_t)tiles;
+    P.table = static_cast<const RayView*>(d_view_table);
+    MESO_CUDA_TRY(cudaMemcpyAsync(d_view_table, host.data(), raymarch_view_table_bytes(n_views),
+                                  cudaMemcpyHostToDevice, st));
+    // the pageable copy above is staged before the call returns
+    const uint32_t blocks = (uint32_t)((tiles + wpc - 1) / wpc);
+    raymarch_kernel<false><<<blocks, wpc * 32, 0, st>>>(P, empty_views);
+  }
+  ctx->launches.fetch_add(1);
+  MESO_CUDA_TRY(cudaGetLastError());
+  return MESO_OK;
+}
+
+}  // namespace meso

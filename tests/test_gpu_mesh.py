@@ -1,0 +1,126 @@
+"""GPU greedy meshing against the CPU oracle (bit-exact after canonical sort).
+
+Quads are packed uint64 whose numeric order is the canonical
+(chunk, dir, z, y, x) order, so parity is np.sort(gpu) == oracle.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import mesoengine_gb300 as meso
+
+pytestmark = pytest.mark.gpu
+
+
+def _sorted(q):
+    return np.sort(np.asarray(q, dtype=np.uint64))
+
+
+def _kat_chunks():
+    c = np.zeros((6, 32, 32, 32), np.uint16)
+    c[0, 5, 6, 7] = 3                                  # single voxel -> 6 unit quads
+    c[1] = 9                                           # full chunk -> 6 quads of 32x32
+    z, y, x = np.indices((32, 32, 32))
+    c[2] = ((x + y + z) % 2 == 0) * 1                  # checkerboard -> no merges
+    c[3] = (x // 4 % 3 + 1) * (z < 20)                 # material stripes
+    c[4, :, :, 31] = 7                                 # wall on the +x border
+    c[5] = np.where((x * 7 + y * 13 + z * 5) % 11 < 5, (x + y) % 3 + 1, 0)
+    return c
+
+
+def test_kat_chunks_u16(ctx):
+    c = _kat_chunks()
+    ref = oracle.mesh_chunks(oracle.SRC_CHUNKS_U16, c)
+    q, counts = ctx.mesh(meso.SRC_CHUNKS_U16, ctx.to_device(c), n=c.shape[0], chunk_counts=True)
+    assert np.array_equal(_sorted(q), ref)
+    per = np.bincount(oracle.unpack_quads(ref)["chunk"], minlength=c.shape[0])
+    assert np.array_equal(counts, per)
+    assert per[0] == 6 and per[1] == 6 and per[2] == 6 * 16384
+
+
+def test_generated_chunks_match_oracle(ctx):
+    n = 48
+    dev, solid = ctx.generate_chunks_u16(n, seed0=1)
+    host, hsolid = oracle.gen_chunks_u16(n, 1)
+    got = dev.download(np.uint16).reshape(n, 32, 32, 32)
+    assert np.array_equal(got, host)
+    assert np.array_equal(solid.download(np.uint32), hsolid)
+    assert np.array_equal((host > 0).reshape(n, -1).sum(1), hsolid)
+
+
+def test_chunks_u16_batched_and_per_launch(ctx):
+    n = 64
+    dev, _ = ctx.generate_chunks_u16(n, seed0=101)
+    host = dev.download(np.uint16).reshape(n, 32, 32, 32)
+    ref = oracle.mesh_chunks(oracle.SRC_CHUNKS_U16, host)
+    q1, _ = ctx.mesh(meso.SRC_CHUNKS_U16, dev, n=n)
+    q2, _ = ctx.mesh(meso.SRC_CHUNKS_U16, dev, n=n, per_launch=True)
+    assert np.array_equal(_sorted(q1), ref)
+    assert np.array_equal(_sorted(q2), ref)
+
+
+def test_chunk_index_list(ctx):
+    n = 16
+    dev, _ = ctx.generate_chunks_u16(n, seed0=7)
+    host = dev.download(np.uint16).reshape(n, 32, 32, 32)
+    order = np.array([5, 3, 3, 15, 0], dtype=np.int32)
+    ref = oracle.mesh_chunks(oracle.SRC_CHUNKS_U16, host[order])
+    q, _ = ctx.mesh(meso.SRC_CHUNKS_U16, dev, coords=order.reshape(-1, 1))
+    assert np.array_equal(_sorted(q), ref)
+
+
+def test_dense_u8_grid_with_neighbours(ctx):
+    # the small plain case: 256^3 uint8, 512 chunks, faces see across chunks
+    g_dev = ctx.generate_dense_u8(256, 256, 256, seed=1)
+    grid = g_dev.download(np.uint8).reshape(256, 256, 256)
+    assert np.array_equal(grid, oracle.gen_dense_u8(256, 256, 256, 1))
+    coords = np.array([(x, y, z) for z in range(8) for y in range(8) for x in range(8)], dtype=np.int32)
+    ref = oracle.mesh_chunks(oracle.SRC_GRID_U8, grid, coords=coords)
+    q, _ = ctx.mesh(meso.SRC_GRID_U8, g_dev, coords=coords, dims=(256, 256, 256))
+    assert np.array_equal(_sorted(q), ref)
+
+
+def test_dense_u16_grid(ctx):
+    rng = np.random.default_rng(3)
+    g = (rng.random((64, 96, 64)) < 0.3) * rng.integers(1, 4, (64, 96, 64))
+    g = g.astype(np.uint16)
+    coords = np.array([(x, y, z) for z in range(2) for y in range(3) for x in range(2)], dtype=np.int32)
+    ref = oracle.mesh_chunks(oracle.SRC_GRID_U16, g, coords=coords)
+    q, _ = ctx.mesh(meso.SRC_GRID_U16, ctx.to_device(g), coords=coords, dims=(64, 96, 64))
+    assert np.array_equal(_sorted(q), ref)
+
+
+def test_overflow_reports_need(ctx):
+    c = _kat_chunks()[2:3]  # checkerboard: 98304 quads
+    with pytest.raises(meso.MesoError) as e:
+        ctx.mesh(meso.SRC_CHUNKS_U16, ctx.to_device(c), n=1, capacity=1000)
+    assert e.value.status == 4
+    q, _ = ctx.mesh(meso.SRC_CHUNKS_U16, ctx.to_device(c), n=1, capacity=1000, check=False)
+    assert len(q) == 1000
+
+
+def test_empty_input(ctx):
+    c = np.zeros((3, 32, 32, 32), np.uint16)
+    q, counts = ctx.mesh(meso.SRC_CHUNKS_U16, ctx.to_device(c), n=3, chunk_counts=True)
+    assert len(q) == 0 and counts.tolist() == [0, 0, 0]
+    q0, _ = ctx.mesh(meso.SRC_CHUNKS_U16, ctx.to_device(c), n=0)
+    assert len(q0) == 0
+
+
+def test_mesh_host_entry(ctx):
+    c = _kat_chunks()
+    ref = oracle.mesh_chunks(oracle.SRC_CHUNKS_U16, c)
+    q = ctx.mesh_host(meso.SRC_CHUNKS_U16, c)
+    assert np.array_equal(_sorted(q), ref)
+
+
+def test_brickmap_chunks(ctx):
+    t = meso.terrain_preset("small")
+    scene = ctx.scene_from_terrain(t)
+    dense = scene.dense()
+    bm = oracle.HostBrickMap.from_dense(dense)
+    coords = np.array([(x, y, z) for z in range(4) for y in range(4) for x in range(4)], dtype=np.int32)
+    ref = oracle.mesh_chunks(oracle.SRC_BRICKMAP, coords=coords, bm=bm)
+    q, _ = ctx.mesh(meso.SRC_BRICKMAP, coords=coords, scene=scene)
+    assert len(ref) > 0
+    assert np.array_equal(_sorted(q), ref)
