@@ -1,0 +1,414 @@
+#!/usr/bin/env python3
+"""Benchmark of the two voxel hot paths on GB300.
+
+Headline step (value): one 1920x1080 frame of the 1024^3 sparse terrain scene
+(8^3 bricks under a 128^3 pointer grid, ~15% solid, uint16 materials),
+primary rays plus one shadow ray per hit towards normalize(0.3, 0.5, 0.8),
+FP32, one plain per-view launch; metric Mrays/s = (primary + shadow rays) / s.
+Also reported on the same line: batched meshing of 4096 standalone 32^3
+uint16 chunks (Gvox/s, persistent kernel vs one launch per chunk), and the
+served raymarch stream (p50/p99 latency, Mrays/s) when available.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N>1 runs independent replicas, one per rank (the path has no exchange step):
+value = rays of all ranks / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s + meshed Gvox/s; served p50/p99 vs per-call launch, bit-exact on 1 GB300"
+FRAME_W, FRAME_H = 1920, 1080
+CAM_ORIGIN = (-300.0, -200.0, 800.0)
+CAM_TARGET = (512.0, 512.0, 512.0)
+L2_FLUSH_BYTES = 512 << 20
+MESH_CHUNKS = 4096
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # replicas only: gloo for the barrier and the max
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def reduce_max(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def count_rays(hits) -> int:
+    # every pixel casts a primary ray; a shadow ray was traced iff it took steps
+    return int(hits.shape[0] + np.count_nonzero(hits["shadow_steps"]))
+
+
+# ------------------------------------------------------------------ our arm
+
+def bench_raymarch(ctx, meso, steps, warmup, dist, clocks):
+    t = meso.terrain_preset("scene1024")
+    scene = ctx.scene_from_terrain(t)
+    cam = meso.camera(CAM_ORIGIN, CAM_TARGET, FRAME_W, FRAME_H)
+    flush = ctx.alloc(L2_FLUSH_BYTES)
+    out = ctx.alloc(FRAME_W * FRAME_H * 24)
+    for _ in range(warmup):
+        ctx.raymarch(scene, cam, out=out, download=False)
+    ctx.sync()
+    hits = out.download(meso.HIT_DTYPE, FRAME_W * FRAME_H)
+    rays = count_rays(hits)
+    evs = [(ctx.event(), ctx.event()) for _ in range(steps)]
+    launches0 = ctx.kernel_launches
+    barrier(dist)
+    ctx.sync()
+    with clocks:
+        for a, b in evs:
+            flush.zero()  # L2 flush outside the event pair
+            ctx.record(a)
+            ctx.raymarch(scene, cam, out=out, download=False)
+            ctx.record(b)
+        ctx.sync()
+    launches = ctx.kernel_launches - launches0
+    barrier(dist)
+    times = [ctx.elapsed_ms(a, b) for a, b in evs]
+    ms = sum(times) / len(times)
+    # end to end through the host-buffer entry point: camera in, hits back to pinned memory
+    pinned = ctx.pinned(FRAME_W * FRAME_H * 24)
+    for _ in range(2):
+        ctx.raymarch_host(scene, cam, out_ptr=pinned.ptr)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ctx.raymarch_host(scene, cam, out_ptr=pinned.ptr)
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / steps
+    e2e_hits = pinned.view(meso.HIT_DTYPE, FRAME_W * FRAME_H)
+    assert np.array_equal(e2e_hits.view(np.uint8), hits.view(np.uint8)), "host entry point disagrees"
+    fetches, bricks, nhits, traversals = ctx.raymarch_stats(scene, cam, out=out)
+    algo_bytes = 4 * fetches + 64 * bricks + 2 * nhits + 24 * FRAME_W * FRAME_H
+    info = scene.info()
+    return {
+        "scene": scene, "cam": cam, "hits": hits, "rays": rays, "ms": ms, "times": times,
+        "launches": launches, "e2e_ms": e2e_ms, "algo_bytes": algo_bytes,
+        "counts": {"pointer_fetches": fetches, "bricks_entered": bricks, "hits": nhits, "traversals": traversals},
+        "bricks": int(info.n_bricks), "scene_bytes": int(info.device_bytes),
+    }
+
+
+def bench_mesh(ctx, meso, steps, warmup):
+    data, _ = ctx.generate_chunks_u16(MESH_CHUNKS, seed0=1)
+    cap = MESH_CHUNKS * 8192
+    qbuf = ctx.alloc(cap * 8)
+    cnt = ctx.alloc(8)
+    flush = ctx.alloc(L2_FLUSH_BYTES)
+    src = meso.MeshSource()
+    src.kind = meso.SRC_CHUNKS_U16
+    src.d_data = data.ptr
+    out = meso.MeshOutput(qbuf.ptr, cap, cnt.ptr, None)
+    L = meso._lib
+    import ctypes
+
+    def run(per_launch=False):
+        fn = L.meso_mesh_chunks_per_launch if per_launch else L.meso_mesh_chunks
+        meso._check(fn(ctx.handle, ctypes.byref(src), None, MESH_CHUNKS, ctypes.byref(out), None))
+
+    for _ in range(warmup):
+        run()
+    ctx.sync()
+    total = ctypes.c_uint64()
+    meso._check(L.meso_mesh_check(ctx.handle, ctypes.byref(out), None, ctypes.byref(total)))
+    quads = int(total.value)
+    evs = [(ctx.event(), ctx.event()) for _ in range(steps)]
+    for a, b in evs:
+        flush.zero()
+        ctx.record(a)
+        run()
+        ctx.record(b)
+    ctx.sync()
+    times = [ctx.elapsed_ms(a, b) for a, b in evs]
+    ms = sum(times) / len(times)
+    # plain form: one launch per chunk
+    run(per_launch=True)
+    ctx.sync()
+    a, b = ctx.event(), ctx.event()
+    flush.zero()
+    ctx.record(a)
+    run(per_launch=True)
+    ctx.record(b)
+    ctx.sync()
+    ms_plain = ctx.elapsed_ms(a, b)
+    meso._check(L.meso_mesh_check(ctx.handle, ctypes.byref(out), None, ctypes.byref(total)))
+    assert int(total.value) == quads
+    vox = MESH_CHUNKS * 32768
+    algo = MESH_CHUNKS * 65536 + 8 * quads
+    return {"ms": ms, "ms_plain": ms_plain, "quads": quads, "gvox_s": vox / (ms * 1e6),
+            "gvox_s_plain": vox / (ms_plain * 1e6), "algo_bytes": algo}
+
+
+def cpu_baseline_port(meso, ctx, r):
+    """Oracle DDA on the host cores over the whole frame, scene copied from the device."""
+    import oracle
+    ptr, occ, mat = r["scene"].download()
+    bm = oracle.HostBrickMap.from_arrays((1024, 1024, 1024), ptr, occ, mat)
+    ocam = oracle.camera(CAM_ORIGIN, CAM_TARGET, FRAME_W, FRAME_H)
+    threads = oracle.hardware_threads()
+    t0 = time.perf_counter()
+    h = oracle.raymarch(bm, ocam, nthreads=threads)
+    dt = time.perf_counter() - t0
+    parity = bool(np.array_equal(h.view(np.uint8), r["hits"].view(np.uint8)))
+    return {"value": count_rays(h) / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"the full {FRAME_W}x{FRAME_H} frame (primary + shadow), {dt:.2f} s",
+            "parity_full_frame_bit_exact": parity}
+
+
+def run_ours(args, world, rank, local, dist):
+    import mesoengine_gb300 as meso
+    ctx = meso.Context(local)
+    clocks = Clocks(local)
+    r = bench_raymarch(ctx, meso, args.steps, args.warmup, dist, clocks)
+    clk = clocks.summary()
+    ms_max = reduce_max(dist, r["ms"])
+    rays_all = reduce_sum(dist, float(r["rays"]))
+    value = rays_all / (ms_max * 1e3)  # Mrays/s
+    hbm, which = peaks()
+    achieved = r["algo_bytes"] / (r["ms"] * 1e6)  # GB/s
+    line = {
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": "Mrays/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_max, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded terrain: 6-octave fBm heightfield + 3-D value-noise caves)",
+        "config": {
+            "workload": "1024^3 sparse brick scene, 1920x1080 primary + 1 shadow ray per hit, plain per-view launch",
+            "scene": "8^3 bricks, 128^3 uint32 pointer grid, uint16 materials, "
+                     f"{r['bricks']} bricks, {r['scene_bytes'] / 2**20:.0f} MiB resident",
+            "camera": {"origin": CAM_ORIGIN, "target": CAM_TARGET, "fov_y_deg": 60},
+            "rays_per_frame": r["rays"],
+            "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB memset outside the timed events)",
+            "parallelism": f"replicas x{world}",
+        },
+        "clocks": clk,
+        "e2e": {"value": round(r["rays"] / (r["e2e_ms"] * 1e3), 2), "unit": "Mrays/s",
+                "h2d_bytes_per_step": 72, "d2h_bytes_per_step": FRAME_W * FRAME_H * 24,
+                "api": "meso_raymarch_host (pinned host hit buffer)"},
+        "gpu_launches": int(r["launches"]),
+        "roofline": {
+            "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "traffic": None, "peak_source": which,
+            "kernel": "raymarch_kernel",
+            "algorithmic_bytes_per_launch": int(r["algo_bytes"]),
+            "counts": r["counts"],
+        },
+    }
+    if rank == 0 and not args.skip_mesh:
+        m = bench_mesh(ctx, meso, args.steps, args.warmup)
+        ach = m["algo_bytes"] / (m["ms"] * 1e6)
+        line["mesh"] = {
+            "workload": f"{MESH_CHUNKS} standalone 32^3 uint16 chunks, occupancy log-uniform 0.1%-90%, 1-64 materials",
+            "gvox_s": round(m["gvox_s"], 2), "ms": round(m["ms"], 4), "quads": m["quads"],
+            "per_chunk_launch_gvox_s": round(m["gvox_s_plain"], 3),
+            "batched_over_per_launch": round(m["ms_plain"] / m["ms"], 2),
+            "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(ach / hbm, 4), "algorithmic_bytes_per_launch": m["algo_bytes"],
+                         "kernel": "mesh_kernel<CHUNKS_U16>"},
+        }
+    if rank == 0 and not args.skip_cpu:
+        line["cpu_baseline"] = cpu_baseline_port(meso, ctx, r)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+# ------------------------------------------------------------ reference arm
+
+def run_reference(args, world, rank, local, dist):
+    """The reference has no raymarcher (it rasterises imposter cubes through
+    Vulkan, which cannot run here); its stand-in is the CPU oracle DDA on all
+    host cores, on the same scene and camera.  Each step traces a bounded
+    sample of 270 rows of the frame."""
+    if rank != 0:
+        return
+    import oracle
+    import mesoengine_gb300 as meso_presets  # parameters only (terrain preset), no device use
+    t = meso_presets.terrain_preset("scene1024")
+    ot = oracle.terrain(t.nx, t.ny, t.nz, t.seed, t.height_period, t.height_octaves, t.height_base, t.height_amp,
+                        t.cave_period, t.cave_threshold)
+    threads = oracle.hardware_threads()
+    bm = oracle.HostBrickMap.from_terrain(ot, nthreads=threads)
+    cam = oracle.camera(CAM_ORIGIN, CAM_TARGET, FRAME_W, FRAME_H)
+    rows = 270
+    for k in range(args.warmup):
+        oracle.raymarch_rows(bm, cam, (k * rows) % FRAME_H, rows, nthreads=threads)
+    total_rays, total_s = 0, 0.0
+    for k in range(args.steps):
+        r0 = (k * rows) % FRAME_H
+        t0 = time.perf_counter()
+        h = oracle.raymarch_rows(bm, cam, r0, rows, nthreads=threads)
+        total_s += time.perf_counter() - t0
+        total_rays += count_rays(h)
+    value = total_rays / total_s / 1e6
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total_s * 1000 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (same seeded 1024^3 terrain and camera)",
+        "config": {"workload": "1024^3 sparse brick scene, 1920x1080 primary + 1 shadow ray per hit",
+                   "sample_rows_per_step": rows},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"{rows} rows of the 1920x1080 frame per step"},
+        "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_profile_case(case: str):
+    """One kernel of interest after a few warm-up launches, for ncu captures:
+    'ray' = the 1080p frame of the 1024^3 scene (3 warm-up launches + 1),
+    'mesh' = the 4096-chunk batched mesh (3 warm-up launches + 1)."""
+    import mesoengine_gb300 as meso
+    ctx = meso.Context(0)
+    if case == "ray":
+        scene = ctx.scene_from_terrain(meso.terrain_preset("scene1024"))
+        cam = meso.camera(CAM_ORIGIN, CAM_TARGET, FRAME_W, FRAME_H)
+        out = ctx.alloc(FRAME_W * FRAME_H * 24)
+        for _ in range(4):
+            ctx.raymarch(scene, cam, out=out, download=False)
+    else:
+        data, _ = ctx.generate_chunks_u16(MESH_CHUNKS, seed0=1)
+        for _ in range(4):
+            ctx.mesh(meso.SRC_CHUNKS_U16, data, n=MESH_CHUNKS, capacity=MESH_CHUNKS * 8192)
+    ctx.sync()
+    print(f"profile case {case} done, {ctx.kernel_launches} launches")
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--profile", choices=["ray", "mesh"], default=None,
+                    help="run one small single-kernel case for an ncu capture and exit")
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-mesh", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.profile:
+        run_profile_case(args.profile)
+        return
+    args.warmup = max(3, args.warmup)
+    world, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank, local, dist)
+    else:
+        run_ours(args, world, rank, local, dist)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -247,6 +247,14 @@ meso_status meso_raymarch_per_view(meso_ctx* ctx, const meso_scene* const* scene
 meso_status meso_raymarch_host(meso_ctx* ctx, const meso_scene* scene, const meso_camera* h_cam,
                                const float light[3], uint32_t flags, meso_hit* h_hits);
 
+/* Same launch as meso_raymarch (at most 32 views) through a separate kernel
+ * instantiation that also counts, over all primary and shadow rays:
+ * h_counts[0] brick-pointer fetches, [1] occupied bricks entered, [2] hits,
+ * [3] rays.  For roofline accounting; the timed path carries no counters. */
+meso_status meso_raymarch_stats(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* h_cams,
+                                uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
+                                uint64_t h_counts[4]);
+
 /* ------------------------------------------------------------------- edits */
 
 typedef struct meso_sphere_edit {

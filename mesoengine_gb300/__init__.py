@@ -167,6 +167,8 @@ _SIGNATURES = {
                                ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p],
     "meso_raymarch_host": [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Camera), ctypes.c_void_p,
                            ctypes.c_uint32, ctypes.c_void_p],
+    "meso_raymarch_stats": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Camera),
+                            ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p],
     "meso_edit_spheres": [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(SphereEdit), ctypes.c_uint32,
                           ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32), ctypes.c_void_p],
     "meso_server_create": [ctypes.c_void_p, ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p),
@@ -252,6 +254,34 @@ class DeviceBuffer:
     def free(self) -> None:
         if self.ptr and _lib is not None:
             _lib.meso_dev_free(self.ctx.handle, self.ptr)
+        self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class PinnedBuffer:
+    """Page-locked host allocation owned by a Context."""
+
+    def __init__(self, ctx: "Context", nbytes: int):
+        self.ctx = ctx
+        self.nbytes = int(nbytes)
+        p = ctypes.c_void_p()
+        _check(_lib.meso_host_alloc_pinned(ctx.handle, max(16, self.nbytes), ctypes.byref(p)))
+        self.ptr = p.value
+
+    def view(self, dtype, count=None) -> np.ndarray:
+        dt = np.dtype(dtype)
+        n = self.nbytes // dt.itemsize if count is None else int(count)
+        buf = (ctypes.c_uint8 * (n * dt.itemsize)).from_address(self.ptr)
+        return np.frombuffer(buf, dtype=dt, count=n)
+
+    def free(self) -> None:
+        if self.ptr and _lib is not None:
+            _lib.meso_host_free_pinned(self.ctx.handle, self.ptr)
         self.ptr = None
 
     def __del__(self):
@@ -469,12 +499,36 @@ class Context:
         self.sync(stream)
         return out.download(HIT_DTYPE, total)
 
-    def raymarch_host(self, scene: Scene, cam: Camera, light=None, shadow=True) -> np.ndarray:
-        hits = np.empty(cam.width * cam.height, dtype=HIT_DTYPE)
+    def raymarch_host(self, scene: Scene, cam: Camera, light=None, shadow=True, out_ptr=None) -> np.ndarray:
+        """Host-buffer entry point; out_ptr (e.g. a PinnedBuffer.ptr) receives the hits."""
         L = np.asarray(light_dir() if light is None else light, dtype=np.float32)
+        hits = None
+        if out_ptr is None:
+            hits = np.empty(cam.width * cam.height, dtype=HIT_DTYPE)
+            out_ptr = hits.ctypes.data
         _check(_lib.meso_raymarch_host(self.handle, scene.handle, ctypes.byref(cam), _np_ptr(L),
-                                       RAY_SHADOW if shadow else 0, _np_ptr(hits)))
+                                       RAY_SHADOW if shadow else 0, ctypes.c_void_p(out_ptr)))
         return hits
+
+    def raymarch_stats(self, scenes, cams, light=None, shadow=True, out: DeviceBuffer | None = None):
+        """(pointer fetches, occupied bricks entered, hits, rays) of one launch."""
+        scenes = scenes if isinstance(scenes, (list, tuple)) else [scenes]
+        cams = cams if isinstance(cams, (list, tuple)) else [cams]
+        if len(scenes) == 1 and len(cams) > 1:
+            scenes = scenes * len(cams)
+        sh = (ctypes.c_void_p * len(scenes))(*[s.handle for s in scenes])
+        ca = (Camera * len(cams))(*cams)
+        total = sum(c.width * c.height for c in cams)
+        if out is None:
+            out = self.alloc(total * 24)
+        L = np.asarray(light_dir() if light is None else light, dtype=np.float32)
+        counts = np.zeros(4, dtype=np.uint64)
+        _check(_lib.meso_raymarch_stats(self.handle, sh, ca, len(cams), _np_ptr(L), RAY_SHADOW if shadow else 0,
+                                        out.ptr, _np_ptr(counts)))
+        return [int(v) for v in counts]
+
+    def pinned(self, nbytes: int) -> PinnedBuffer:
+        return PinnedBuffer(self, nbytes)
 
     def autotune(self, path: str | None = None) -> None:
         _check(_lib.meso_autotune(self.handle, path.encode() if path else None))

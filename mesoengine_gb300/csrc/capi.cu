@@ -415,6 +415,25 @@ meso_status meso_raymarch_host(meso_ctx* ctx, const meso_scene* scene, const mes
   return rc;
 }
 
+meso_status meso_raymarch_stats(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* cams,
+                                uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
+                                uint64_t h_counts[4]) {
+  if (!ctx || !h_counts) return fail(MESO_ERR_INVALID_ARG, "raymarch_stats: null argument");
+  if (n_views > 32) return fail(MESO_ERR_INVALID_ARG, "raymarch_stats: at most 32 views");
+  cudaStream_t st = ctx->stream;
+  uint64_t* d = nullptr;
+  MESO_CUDA_TRY(cudaMallocAsync(&d, 32, st));
+  MESO_CUDA_TRY(cudaMemsetAsync(d, 0, 32, st));
+  meso_status rc = launch_raymarch(ctx, scenes, cams, n_views, light, flags, d_hits, st, nullptr, 0, d);
+  if (rc == MESO_OK) {
+    cudaError_t e = cudaMemcpyAsync(h_counts, d, 32, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "raymarch_stats");
+  }
+  cudaFreeAsync(d, st);
+  return rc;
+}
+
 // ------------------------------------------------------------------- edits
 
 meso_status meso_edit_spheres(meso_ctx* ctx, meso_scene* scene, const meso_sphere_edit* h_spheres, uint32_t n,

@@ -98,7 +98,8 @@ meso_status launch_mesh(meso_ctx* ctx, const meso_mesh_source* src, const int32_
 struct RayView;
 meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* cams,
                             uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
-                            cudaStream_t st, void* d_view_table, size_t view_table_bytes);
+                            cudaStream_t st, void* d_view_table, size_t view_table_bytes,
+                            uint64_t* d_stats = nullptr);
 size_t raymarch_view_table_bytes(uint32_t n_views);
 
 }  // namespace meso

@@ -54,6 +54,7 @@ struct RayParams {
   float light[3];
   uint32_t shadow;
   meso_hit* hits;
+  uint64_t* stats;
 };
 
 struct Trav {
@@ -62,6 +63,7 @@ struct Trav {
   float t;
   int axis;
   uint32_t coarse, fine;
+  uint32_t fetches, bricks;  // pointer fetches and occupied bricks entered (statistics only)
 };
 
 __device__ __forceinline__ float bound_time(int b, float o, float inv) {
@@ -73,9 +75,18 @@ __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? l
 // Walks from voxel (vx,vy,vz) (absolute, inside the grid) at time t, entered
 // through axis ea (-1 none).  Ray coordinates are relative to the absolute
 // voxel (bx0,by0,bz0).
+//
+// The walk is the same sequence of float operations as a step-by-step
+// recomputation, organised for issue efficiency: a boundary time is only
+// recomputed for the axis that stepped (the others are unchanged values),
+// the entry voxel of a brick is derived only when an occupied brick is
+// reached, the pointer index is stepped incrementally, and the occupancy
+// word of the current z layer stays in a register.
+template <bool kStats>
 __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int bz0, float ox, float oy, float oz,
                                          float dx, float dy, float dz, int vx, int vy, int vz, float t, int ea,
                                          Trav& r) {
+  uint32_t n_fetch = 0, n_brick = 0;
   const int sx = dx > 0.0f ? 1 : (dx < 0.0f ? -1 : 0);
   const int sy = dy > 0.0f ? 1 : (dy < 0.0f ? -1 : 0);
   const int sz = dz > 0.0f ? 1 : (dz < 0.0f ? -1 : 0);
@@ -84,81 +95,126 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
   const float iz = sz ? __fdiv_rn(1.0f, dz) : 0.0f;
   const int px = sx > 0 ? 1 : 0, py = sy > 0 ? 1 : 0, pz = sz > 0 ? 1 : 0;
   const int NBx = V.nx >> 3, NBy = V.ny >> 3, NBz = V.nz >> 3;
+  const uint32_t strideY = (uint32_t)NBx, strideZ = (uint32_t)NBx * (uint32_t)NBy;
+  // signed index increments of one step along each axis
+  const uint32_t dIx = (uint32_t)sx, dIy = (uint32_t)(sy * (int)strideY), dIz = (uint32_t)(sz * (int)strideZ);
   int Bx = vx >> 3, By = vy >> 3, Bz = vz >> 3;
+  uint32_t idx = (uint32_t)Bx + strideY * (uint32_t)By + strideZ * (uint32_t)Bz;
   uint32_t cs = 0, fs = 0;
   const uint32_t cap = (uint32_t)(4 * (V.nx + V.ny + V.nz) + 64);
   r.hit = 0;
   for (;;) {
     if (cs + fs > cap) break;
-    const uint32_t p = __ldg(V.ptr + (size_t)Bx + (size_t)NBx * ((size_t)By + (size_t)NBy * (size_t)Bz));
-    if (p == MESO_EMPTY_BRICK) {
-      const float tx = sx ? bound_time((Bx + px) * 8 - bx0, ox, ix) : kInf;
-      const float ty = sy ? bound_time((By + py) * 8 - by0, oy, iy) : kInf;
-      const float tz = sz ? bound_time((Bz + pz) * 8 - bz0, oz, iz) : kInf;
-      int a = 0;
-      float tm = tx;
-      if (ty < tm) { a = 1; tm = ty; }
-      if (tz < tm) { a = 2; tm = tz; }
-      cs++;
-      t = tm;
-      ea = a;
-      bool out;
-      if (a == 0) {
-        Bx += sx;
-        out = Bx < 0 || Bx >= NBx;
-        vx = sx > 0 ? Bx * 8 : Bx * 8 + 7;
-        vy = clampi((int)floorf(__fadd_rn(oy, __fmul_rn(dy, t))) + by0, By * 8, By * 8 + 7);
-        vz = clampi((int)floorf(__fadd_rn(oz, __fmul_rn(dz, t))) + bz0, Bz * 8, Bz * 8 + 7);
-      } else if (a == 1) {
-        By += sy;
-        out = By < 0 || By >= NBy;
-        vy = sy > 0 ? By * 8 : By * 8 + 7;
-        vx = clampi((int)floorf(__fadd_rn(ox, __fmul_rn(dx, t))) + bx0, Bx * 8, Bx * 8 + 7);
-        vz = clampi((int)floorf(__fadd_rn(oz, __fmul_rn(dz, t))) + bz0, Bz * 8, Bz * 8 + 7);
-      } else {
-        Bz += sz;
-        out = Bz < 0 || Bz >= NBz;
-        vz = sz > 0 ? Bz * 8 : Bz * 8 + 7;
-        vx = clampi((int)floorf(__fadd_rn(ox, __fmul_rn(dx, t))) + bx0, Bx * 8, Bx * 8 + 7);
-        vy = clampi((int)floorf(__fadd_rn(oy, __fmul_rn(dy, t))) + by0, By * 8, By * 8 + 7);
-      }
-      if (out) break;
-      continue;
+    uint32_t p = __ldg(V.ptr + idx);
+    if (kStats) {
+      n_fetch++;
+      n_brick += p != MESO_EMPTY_BRICK;
     }
+    if (p == MESO_EMPTY_BRICK) {
+      // ---- coarse: one step per empty brick; nb* = next brick boundary
+      // (relative voxel coordinate) along each axis
+      int nbx = (Bx + px) * 8 - bx0, nby = (By + py) * 8 - by0, nbz = (Bz + pz) * 8 - bz0;
+      float tx = sx ? bound_time(nbx, ox, ix) : kInf;
+      float ty = sy ? bound_time(nby, oy, iy) : kInf;
+      float tz = sz ? bound_time(nbz, oz, iz) : kInf;
+      bool out = false;
+      int a;
+      for (;;) {
+        const bool cy = ty < tx;
+        float tm = cy ? ty : tx;
+        const bool cz = tz < tm;
+        tm = cz ? tz : tm;
+        a = cz ? 2 : (cy ? 1 : 0);
+        cs++;
+        t = tm;
+        const bool a0 = a == 0, a1 = a == 1, a2 = a == 2;
+        Bx += a0 ? sx : 0;
+        By += a1 ? sy : 0;
+        Bz += a2 ? sz : 0;
+        idx += a0 ? dIx : (a1 ? dIy : dIz);
+        out = ((unsigned)Bx >= (unsigned)NBx) | ((unsigned)By >= (unsigned)NBy) | ((unsigned)Bz >= (unsigned)NBz);
+        if (out || cs + fs > cap) break;
+        p = __ldg(V.ptr + idx);
+        if (kStats) {
+          n_fetch++;
+          n_brick += p != MESO_EMPTY_BRICK;
+        }
+        if (p != MESO_EMPTY_BRICK) break;
+        nbx += a0 ? 8 * sx : 0;
+        nby += a1 ? 8 * sy : 0;
+        nbz += a2 ? 8 * sz : 0;
+        const int nb = a0 ? nbx : (a1 ? nby : nbz);
+        const float oo = a0 ? ox : (a1 ? oy : oz);
+        const float ii = a0 ? ix : (a1 ? iy : iz);
+        const float tn = bound_time(nb, oo, ii);
+        tx = a0 ? tn : tx;
+        ty = a1 ? tn : ty;
+        tz = a2 ? tn : tz;
+      }
+      ea = a;
+      if (out || p == MESO_EMPTY_BRICK) break;
+      // entry voxel of the occupied brick: exact along the stepped axis,
+      // floor of the entry point (clamped into the brick) along the others
+      const int fx = clampi((int)floorf(__fadd_rn(ox, __fmul_rn(dx, t))) + bx0, Bx * 8, Bx * 8 + 7);
+      const int fy = clampi((int)floorf(__fadd_rn(oy, __fmul_rn(dy, t))) + by0, By * 8, By * 8 + 7);
+      const int fz = clampi((int)floorf(__fadd_rn(oz, __fmul_rn(dz, t))) + bz0, Bz * 8, Bz * 8 + 7);
+      vx = a == 0 ? (sx > 0 ? Bx * 8 : Bx * 8 + 7) : fx;
+      vy = a == 1 ? (sy > 0 ? By * 8 : By * 8 + 7) : fy;
+      vz = a == 2 ? (sz > 0 ? Bz * 8 : Bz * 8 + 7) : fz;
+    }
+    // ---- fine: voxel steps inside occupied brick p; nv* = next voxel
+    // boundary (relative) along each axis
+    if (cs + fs > cap) break;
     const uint64_t* occ = V.occ + (size_t)p * 8;
-    bool left = false;
+    uint64_t w = __ldg(occ + (vz & 7));
+    int nvx = vx + px - bx0, nvy = vy + py - by0, nvz = vz + pz - bz0;
+    float tx = sx ? bound_time(nvx, ox, ix) : kInf;
+    float ty = sy ? bound_time(nvy, oy, iy) : kInf;
+    float tz = sz ? bound_time(nvz, oz, iz) : kInf;
+    bool left = false, exit_brick = false;
     for (;;) {
-      const uint64_t w = __ldg(occ + (vz & 7));
       if ((w >> ((vx & 7) + 8 * (vy & 7))) & 1ull) {
         r.hit = 1;
         break;
       }
-      const float tx = sx ? bound_time(vx + px - bx0, ox, ix) : kInf;
-      const float ty = sy ? bound_time(vy + py - by0, oy, iy) : kInf;
-      const float tz = sz ? bound_time(vz + pz - bz0, oz, iz) : kInf;
-      int a = 0;
-      float tm = tx;
-      if (ty < tm) { a = 1; tm = ty; }
-      if (tz < tm) { a = 2; tm = tz; }
+      const bool cy = ty < tx;
+      float tm = cy ? ty : tx;
+      const bool cz = tz < tm;
+      tm = cz ? tz : tm;
+      const int a = cz ? 2 : (cy ? 1 : 0);
       fs++;
       t = tm;
       ea = a;
-      bool exit_brick;
-      if (a == 0) {
-        vx += sx;
-        exit_brick = (vx >> 3) != Bx;
-        if (exit_brick) { Bx += sx; left = Bx < 0 || Bx >= NBx; }
-      } else if (a == 1) {
-        vy += sy;
-        exit_brick = (vy >> 3) != By;
-        if (exit_brick) { By += sy; left = By < 0 || By >= NBy; }
-      } else {
-        vz += sz;
-        exit_brick = (vz >> 3) != Bz;
-        if (exit_brick) { Bz += sz; left = Bz < 0 || Bz >= NBz; }
+      const bool a0 = a == 0, a1 = a == 1, a2 = a == 2;
+      vx += a0 ? sx : 0;
+      vy += a1 ? sy : 0;
+      vz += a2 ? sz : 0;
+      const int c = a0 ? vx : (a1 ? vy : vz);
+      const int cb = a0 ? Bx : (a1 ? By : Bz);
+      exit_brick = (c >> 3) != cb;
+      if (exit_brick) {
+        Bx = vx >> 3;
+        By = vy >> 3;
+        Bz = vz >> 3;
+        idx += a0 ? dIx : (a1 ? dIy : dIz);
+        left = ((unsigned)Bx >= (unsigned)NBx) | ((unsigned)By >= (unsigned)NBy) | ((unsigned)Bz >= (unsigned)NBz);
+        break;
       }
-      if (exit_brick) break;
-      if (cs + fs > cap) { left = true; break; }
+      nvx += a0 ? sx : 0;
+      nvy += a1 ? sy : 0;
+      nvz += a2 ? sz : 0;
+      const int nv = a0 ? nvx : (a1 ? nvy : nvz);
+      const float oo = a0 ? ox : (a1 ? oy : oz);
+      const float ii = a0 ? ix : (a1 ? iy : iz);
+      const float tn = bound_time(nv, oo, ii);
+      tx = a0 ? tn : tx;
+      ty = a1 ? tn : ty;
+      tz = a2 ? tn : tz;
+      if (a2) w = __ldg(occ + (vz & 7));
+      if (cs + fs > cap) {
+        left = true;
+        break;
+      }
     }
     if (r.hit || left) break;
   }
@@ -169,6 +225,8 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
   r.axis = ea;
   r.coarse = cs;
   r.fine = fs;
+  r.fetches = n_fetch;
+  r.bricks = n_brick;
 }
 
 __device__ __forceinline__ void camera_ray(const RayView& V, uint32_t px, uint32_t py, float& dx, float& dy,
@@ -194,8 +252,9 @@ __device__ __forceinline__ void camera_ray(const RayView& V, uint32_t px, uint32
   dz = __fdiv_rn(d2, len);
 }
 
+template <bool kStats>
 __device__ __forceinline__ void trace_pixel(const RayView& V, uint32_t px, uint32_t py, const RayParams& P,
-                                            meso_hit& h) {
+                                            meso_hit& h, uint32_t* st) {
   h.voxel = ~0ull;
   h.t = kInf;
   h.material = 0;
@@ -268,9 +327,15 @@ __device__ __forceinline__ void trace_pixel(const RayView& V, uint32_t px, uint3
     vz = clampi((int)floorf(oz) + bz0, 0, V.nz - 1);
   }
   Trav r;
-  traverse(V, bx0, by0, bz0, ox, oy, oz, dx, dy, dz, vx, vy, vz, t0, ea, r);
+  traverse<kStats>(V, bx0, by0, bz0, ox, oy, oz, dx, dy, dz, vx, vy, vz, t0, ea, r);
   h.steps = r.fine | (r.coarse << 16);
+  if (kStats) {
+    st[0] += r.fetches;
+    st[1] += r.bricks;
+    st[3] += 1;
+  }
   if (!r.hit) return;
+  if (kStats) st[2] += 1;
   h.voxel = (uint64_t)r.vx + (uint64_t)V.nx * ((uint64_t)r.vy + (uint64_t)V.ny * (uint64_t)r.vz);
   h.t = r.t;
   {
@@ -292,7 +357,12 @@ __device__ __forceinline__ void trace_pixel(const RayView& V, uint32_t px, uint3
     return;
   }
   Trav sr;
-  traverse(V, Sx, Sy, Sz, 0.5f, 0.5f, 0.5f, P.light[0], P.light[1], P.light[2], Sx, Sy, Sz, 0.0f, -1, sr);
+  traverse<kStats>(V, Sx, Sy, Sz, 0.5f, 0.5f, 0.5f, P.light[0], P.light[1], P.light[2], Sx, Sy, Sz, 0.0f, -1, sr);
+  if (kStats) {
+    st[0] += sr.fetches;
+    st[1] += sr.bricks;
+    st[3] += 1;
+  }
   h.shadow = (uint8_t)(sr.hit ? 1 : 0);
   h.shadow_steps = sr.fine | (sr.coarse << 16);
 }
@@ -307,7 +377,9 @@ __device__ __forceinline__ void store_hit(meso_hit* dst, const meso_hit& h) {
   d[2] = w2;
 }
 
-template <bool kInline>
+// kStats: also accumulates {pointer fetches, occupied bricks entered, hits,
+// rays} into P.stats (a separate instantiation; the timed path has none of it).
+template <bool kInline, bool kStats>
 __global__ void __launch_bounds__(256) raymarch_kernel(const RayParams P, const __grid_constant__ InlineViews iv) {
   const uint32_t warps = blockDim.x >> 5;
   const uint32_t tile = blockIdx.x * warps + (threadIdx.x >> 5);
@@ -326,10 +398,18 @@ __global__ void __launch_bounds__(256) raymarch_kernel(const RayParams P, const 
   const uint32_t tx = lt % V.tiles_x, ty = lt / V.tiles_x;
   const uint32_t px = tx * P.tile_w + (uint32_t)lane % P.tile_w;
   const uint32_t py = ty * P.tile_h + (uint32_t)lane / P.tile_w;
-  if (px >= V.width || py >= V.height) return;
-  meso_hit h;
-  trace_pixel(V, px, py, P, h);
-  store_hit(P.hits + V.hit_offset + (uint64_t)py * V.width + px, h);
+  uint32_t st[4] = {0, 0, 0, 0};
+  if (px < V.width && py < V.height) {
+    meso_hit h;
+    trace_pixel<kStats>(V, px, py, P, h, st);
+    store_hit(P.hits + V.hit_offset + (uint64_t)py * V.width + px, h);
+  }
+  if (kStats) {
+    for (int k = 0; k < 4; k++) {
+      const uint32_t tot = __reduce_add_sync(0xFFFFFFFFu, st[k]);
+      if (lane == 0) atomicAdd(reinterpret_cast<unsigned long long*>(P.stats) + k, (unsigned long long)tot);
+    }
+  }
 }
 
 }  // namespace
@@ -373,7 +453,7 @@ static uint64_t fill_views(const meso_scene* const* scenes, const meso_camera* c
 
 meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* cams,
                             uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
-                            cudaStream_t st, void* d_view_table, size_t view_table_bytes) {
+                            cudaStream_t st, void* d_view_table, size_t view_table_bytes, uint64_t* d_stats) {
   if (!scenes || !cams || !d_hits) return fail(MESO_ERR_INVALID_ARG, "raymarch: null argument");
   if (n_views == 0) return MESO_OK;
   for (uint32_t v = 0; v < n_views; v++) {
@@ -395,6 +475,7 @@ meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, cons
   if (light)
     for (int a = 0; a < 3; a++) P.light[a] = light[a];
   P.hits = d_hits;
+  P.stats = d_stats;
   static InlineViews empty_views;  // zero-initialised
   uint64_t tiles;
   if (n_views <= (uint32_t)kInlineViews) {
@@ -403,7 +484,8 @@ meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, cons
     if (tiles >= (1ull << 31)) return fail(MESO_ERR_INVALID_ARG, "raymarch: too many tiles");
     P.total_tiles = (uint32_t)tiles;
     const uint32_t blocks = (uint32_t)((tiles + wpc - 1) / wpc);
-    raymarch_kernel<true><<<blocks, wpc * 32, 0, st>>>(P, iv);
+    if (d_stats) raymarch_kernel<true, true><<<blocks, wpc * 32, 0, st>>>(P, iv);
+    else raymarch_kernel<true, false><<<blocks, wpc * 32, 0, st>>>(P, iv);
   } else {
     if (!d_view_table || view_table_bytes < raymarch_view_table_bytes(n_views))
       return fail(MESO_ERR_INVALID_ARG, "raymarch: view table too small");
@@ -416,7 +498,8 @@ meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, cons
                                   cudaMemcpyHostToDevice, st));
     // the pageable copy above is staged before the call returns
     const uint32_t blocks = (uint32_t)((tiles + wpc - 1) / wpc);
-    raymarch_kernel<false><<<blocks, wpc * 32, 0, st>>>(P, empty_views);
+    if (d_stats) raymarch_kernel<false, true><<<blocks, wpc * 32, 0, st>>>(P, empty_views);
+    else raymarch_kernel<false, false><<<blocks, wpc * 32, 0, st>>>(P, empty_views);
   }
   ctx->launches.fetch_add(1);
   MESO_CUDA_TRY(cudaGetLastError());

@@ -495,9 +495,9 @@ static meso_status alloc_sized(meso_ctx* ctx, int32_t nx, int32_t ny, int32_t nz
 
 meso_status scene_create_terrain(meso_ctx* ctx, const meso_terrain* t, uint64_t spare, meso_scene** out) {
   if (!t || !out) return fail(MESO_ERR_INVALID_ARG, "terrain: null argument");
-  if (t->nx <= 0 || t->ny <= 0 || t->nz <= 0 || t->nx % 32 || t->ny % 32 || t->nz % 32 || t->nx > 16384 ||
-      t->ny > 16384 || t->nz > 16384)
-    return fail(MESO_ERR_INVALID_ARG, "terrain: dims must be positive multiples of 32 (<= 16384)");
+  if (t->nx <= 0 || t->ny <= 0 || t->nz <= 0 || t->nx % 32 || t->ny % 32 || t->nz % 32 || t->nx > 8192 ||
+      t->ny > 8192 || t->nz > 8192)
+    return fail(MESO_ERR_INVALID_ARG, "terrain: dims must be positive multiples of 32 (<= 8192)");
   if (t->height_period == 0 || t->cave_period == 0 || t->height_octaves < 1 || t->height_octaves > 16)
     return fail(MESO_ERR_INVALID_ARG, "terrain: bad noise parameters");
   cudaStream_t st = ctx->stream;
@@ -544,8 +544,8 @@ meso_status scene_create_terrain(meso_ctx* ctx, const meso_terrain* t, uint64_t 
 meso_status scene_create_dense(meso_ctx* ctx, const uint16_t* h_grid, int32_t nx, int32_t ny, int32_t nz,
                                uint64_t spare, meso_scene** out) {
   if (!h_grid || !out) return fail(MESO_ERR_INVALID_ARG, "dense scene: null argument");
-  if (nx <= 0 || ny <= 0 || nz <= 0 || nx % 32 || ny % 32 || nz % 32)
-    return fail(MESO_ERR_INVALID_ARG, "dense scene: dims must be positive multiples of 32");
+  if (nx <= 0 || ny <= 0 || nz <= 0 || nx % 32 || ny % 32 || nz % 32 || nx > 8192 || ny > 8192 || nz > 8192)
+    return fail(MESO_ERR_INVALID_ARG, "dense scene: dims must be positive multiples of 32 (<= 8192)");
   cudaStream_t st = ctx->stream;
   const uint64_t nvox = (uint64_t)nx * ny * nz;
   const uint64_t nb = nvox / 512;

@@ -208,6 +208,23 @@ class HostBrickMap:
             raise RuntimeError(f"mo_build_from_dense_u16 failed: {rc}")
         return cls(bm)
 
+    @classmethod
+    def from_arrays(cls, dims, ptr: np.ndarray, occ: np.ndarray, mat: np.ndarray) -> "HostBrickMap":
+        """Wraps existing arrays (e.g. a scene copied back from the device);
+        the arrays stay owned by numpy."""
+        obj = cls.__new__(cls)
+        obj._keep = (np.ascontiguousarray(ptr, dtype=np.uint32), np.ascontiguousarray(occ, dtype=np.uint64),
+                     np.ascontiguousarray(mat, dtype=np.uint16))
+        bm = BrickMap()
+        bm.nx, bm.ny, bm.nz = dims
+        bm.ptr = obj._keep[0].ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        bm.occ = obj._keep[1].ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+        bm.mat = obj._keep[2].ctypes.data_as(ctypes.POINTER(ctypes.c_uint16))
+        bm.n_bricks = bm.cap_bricks = obj._keep[1].shape[0]
+        obj.bm = bm
+        obj._borrowed = True
+        return obj
+
     @property
     def dims(self):
         return (self.bm.nx, self.bm.ny, self.bm.nz)
@@ -252,6 +269,8 @@ class HostBrickMap:
         return out[:n].copy()
 
     def __del__(self):
+        if getattr(self, "_borrowed", False):
+            return
         if getattr(self, "bm", None) is not None and _lib is not None:
             _lib.mo_brickmap_free(ctypes.byref(self.bm))
             self.bm = None
