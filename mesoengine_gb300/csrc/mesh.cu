@@ -35,12 +35,12 @@ namespace {
 
 using namespace ::meso::dev;
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kGreedyWarps = 6;
 constexpr int kS = 33;               // padded row stride of 32x32 word arrays
 constexpr int kArr = 32 * kS;
-constexpr int kQBuf = 512;           // staged quads per greedy warp
+constexpr int kQBuf = 256;           // staged quads per greedy warp
 constexpr int kBrickSlot = 1040;     // bytes per staged brick (bank-spread padding)
 constexpr int kMatBuf = 64 * kBrickSlot;
 constexpr uint32_t kFull = 0xFFFFFFFFu;
@@ -52,6 +52,7 @@ struct __align__(128) MeshSmem {
   uint32_t ex[kArr], ey[kArr], ez[kArr];  // equality with -x / -y / -z neighbour, bits over x, [z][y]
   uint32_t eyt[kArr], ezt[kArr];          // equality with -y / -z neighbour, bits over y, [z][x]
   uint32_t f[6][kArr];                    // face masks; X: [z][x] bits y; Y,Z: [z][y] bits x
+  uint32_t iso[6][kArr];                  // faces linked to no same-material face: 1x1 quads
   uint32_t halo[6][32];                   // -X,+X: bits y by z; -Y,+Y: bits x by z; -Z,+Z: bits x by y
   uint64_t qbuf[kGreedyWarps][kQBuf];
   uint64_t bar[2];
@@ -59,6 +60,11 @@ struct __align__(128) MeshSmem {
   int32_t valid[2];
   int32_t coord[2][3];
   uint32_t chunk_quads;
+  uint32_t iso_count[192];           // isolated quads per word group g = 32*dir + row
+  uint32_t iso_off[192];             // their exclusive prefix within the chunk
+  unsigned long long iso_base;       // global offset of the chunk's isolated quads
+  uint32_t task_next;                // dynamic task counter of pass 4
+  uint32_t qcount[kGreedyWarps];     // staged quads in qbuf[d]
 };
 
 struct MeshParams {
@@ -285,6 +291,30 @@ __device__ __forceinline__ void flush_quads(uint64_t* qb, uint32_t& cnt, const M
   cnt = 0;
 }
 
+// In-register 32x32 bit transpose across a warp: lane r holds row r (bit c =
+// element (r, c)); afterwards lane c holds column c (bit r).  Five butterfly
+// stages swap the off-diagonal blocks of size 16, 8, 4, 2, 1.
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
+#pragma unroll
+  for (int j = 16; j >= 1; j >>= 1) {
+    const uint32_t lo = j == 16 ? 0x0000FFFFu : j == 8 ? 0x00FF00FFu : j == 4 ? 0x0F0F0F0Fu : j == 2 ? 0x33333333u
+                                                                                                      : 0x55555555u;
+    const uint32_t t = __shfl_xor_sync(kFull, x, j);
+    x = (lane & j) ? ((x & ~lo) | ((t & ~lo) >> j)) : ((x & lo) | ((t & lo) << j));
+  }
+  return x;
+}
+
+// Array addressing of direction d: (slice s, row v) -> word offset.
+__device__ __forceinline__ int word_off(int d, int s, int v) { return d < 4 ? v * kS + s : s * kS + v; }
+
+// Origin voxel of a face at (dir d, slice s, column u, row v).
+__device__ __forceinline__ void face_xyz(int d, int s, int u, int v, int& x, int& y, int& z) {
+  if (d < 2) { x = s; y = u; z = v; }
+  else if (d < 4) { x = u; y = s; z = v; }
+  else { x = u; y = v; z = s; }
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(kThreads, 1)
     mesh_kernel(const MeshParams p, const __grid_constant__ CUtensorMap tmap) {
@@ -301,16 +331,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     mbar_init(&sm.bar[0], 1);
     mbar_init(&sm.bar[1], 1);
     sm.chunk_quads = 0;
-    for (int f = 0; f < 6; f++)
-      for (int k = 0; k < 32; k++) sm.halo[f][k] = 0;
     fence_proxy_async_smem();
   }
+  for (int i = tid; i < 6 * 32; i += kThreads) (&sm.halo[0][0])[i] = 0;
+  if (tid < 192) sm.iso_count[tid] = 0;
+  if (tid < kGreedyWarps) sm.qcount[tid] = 0;
+  if (tid == 0) sm.task_next = 0;
   __syncthreads();
   if (warp == 0) issue_chunk<KIND>(sm, p, &tmap, 0, lane, cur, end);
   __syncthreads();
 
   uint32_t phase = 0;  // bit b = parity of buffer b
-  uint32_t qcnt = 0;   // staged quads of this warp (greedy warps)
   int buf = 0;
   for (;;) {
     const int c = sm.chunk[buf];
@@ -336,49 +367,54 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     if (valid) {
       const uint8_t* mb = sm.mat[buf];
-      // ---- pass 1: row masks (lanes = x) ----
+      // ---- pass 1: per z slab (lanes = x): row words by ballot, captured by
+      // lane y; Y faces by shuffles; X-face columns by warp transposes.
       for (int z = warp; z < 32; z += kWarps) {
-        uint32_t occT = 0, eyT = 0, ezT = 0, prev_m = 0, prev_occ = 0;
-        const uint32_t hym = sm.halo[2][z], hyp = sm.halo[3][z];
+        uint32_t r_occ = 0, r_ex = 0, r_ey = 0, r_ez = 0, prev_m = 0;
 #pragma unroll 4
         for (int y = 0; y < 32; y++) {
           const uint32_t m = load_mat<KIND>(mb, lane, y, z);
-          const uint32_t mz = z > 0 ? load_mat<KIND>(mb, lane, y, z - 1) : 0u;
-          const bool solid = m != 0;
-          const uint32_t ml = __shfl_up_sync(kFull, m, 1);
-          const bool bx = m == ml, by = m == prev_m, bz = m == mz;
-          const uint32_t occw = __ballot_sync(kFull, solid);
-          const uint32_t exw = __ballot_sync(kFull, bx);
-          const uint32_t eyw = __ballot_sync(kFull, by);
-          const uint32_t ezw = __ballot_sync(kFull, bz);
-          occT |= (uint32_t)solid << y;
-          eyT |= (uint32_t)by << y;
-          ezT |= (uint32_t)bz << y;
-          const int o = z * kS + y;
-          switch (lane) {
-            case 0: sm.occ[o] = occw; break;
-            case 1: sm.ex[o] = exw; break;
-            case 2: sm.ey[o] = eyw; break;
-            case 3: sm.ez[o] = ezw; break;
-            case 4: sm.f[3][o] = occw & ~(y > 0 ? prev_occ : hym); break;
-            case 5: if (y > 0) sm.f[2][o - 1] = prev_occ & ~occw; break;
-            case 6: if (y == 31) sm.f[2][o] = occw & ~hyp; break;
-            default: break;
+          const uint32_t occw = __ballot_sync(kFull, m != 0);
+          if (lane == y) r_occ = occw;
+          if (occw) {  // equality bits only matter on solid voxels
+            const uint32_t mz = z > 0 ? load_mat<KIND>(mb, lane, y, z - 1) : 0u;
+            const uint32_t ml = __shfl_up_sync(kFull, m, 1);
+            const uint32_t exw = __ballot_sync(kFull, m == ml);
+            const uint32_t eyw = __ballot_sync(kFull, m == prev_m);
+            const uint32_t ezw = __ballot_sync(kFull, m == mz);
+            if (lane == y) {
+              r_ex = exw;
+              r_ey = eyw;
+              r_ez = ezw;
+            }
           }
           prev_m = m;
-          prev_occ = occw;
         }
+        const int o = z * kS + lane;
+        sm.occ[o] = r_occ;
+        sm.ex[o] = r_ex;
+        sm.ey[o] = r_ey;
+        sm.ez[o] = r_ez;
+        {
+          uint32_t up = __shfl_down_sync(kFull, r_occ, 1), dn = __shfl_up_sync(kFull, r_occ, 1);
+          if (lane == 31) up = sm.halo[3][z];
+          if (lane == 0) dn = sm.halo[2][z];
+          sm.f[2][o] = r_occ & ~up;  // +Y, [z][y]
+          sm.f[3][o] = r_occ & ~dn;  // -Y
+        }
+        const uint32_t occT = transpose32(r_occ, lane);
+        const uint32_t eyT = transpose32(r_ey, lane);
+        const uint32_t ezT = transpose32(r_ez, lane);
         uint32_t up = __shfl_down_sync(kFull, occT, 1), dn = __shfl_up_sync(kFull, occT, 1);
         if (lane == 31) up = sm.halo[1][z];
         if (lane == 0) dn = sm.halo[0][z];
-        const int o = z * kS + lane;
-        sm.f[0][o] = occT & ~up;
-        sm.f[1][o] = occT & ~dn;
+        sm.f[0][o] = occT & ~up;  // +X, [z][x] bits y
+        sm.f[1][o] = occT & ~dn;  // -X
         sm.eyt[o] = eyT;
         sm.ezt[o] = ezT;
       }
       __syncthreads();
-      // ---- pass 2: +Z / -Z face masks ----
+      // ---- pass 2: +Z / -Z face masks
       for (int i = tid; i < 1024; i += kThreads) {
         const int z = i >> 5, y = i & 31, o = z * kS + y;
         const uint32_t oc = sm.occ[o];
@@ -388,76 +424,177 @@ __global__ void __launch_bounds__(kThreads, 1)
         sm.f[5][o] = oc & ~dn;
       }
       __syncthreads();
-      // ---- pass 3: greedy, warp = direction, lane = slice ----
-      if (warp < kGreedyWarps) {
-        const int dir = warp, s = lane;
-        uint32_t* F = sm.f[dir];
-        const uint32_t* E;
-        const uint32_t* V;
-        int ss, sv;
-        if (dir < 2) {
-          E = sm.eyt; V = sm.ezt; ss = 1; sv = kS;
-        } else if (dir < 4) {
-          E = sm.ex; V = sm.ez; ss = 1; sv = kS;
-        } else {
-          E = sm.ex; V = sm.ey; ss = kS; sv = 1;
+      // ---- pass 3: isolated faces (no same-material face neighbour in the
+      // plane).  Every greedy scan emits them as 1x1 quads and no other quad
+      // touches them, so they are peeled off and emitted in bulk.
+      for (int i = tid; i < 6 * 1024; i += kThreads) {
+        const int d = i >> 10, v = (i >> 5) & 31, sl = i & 31;
+        const int o = word_off(d, sl, v), sv = d < 4 ? kS : 1;
+        const uint32_t* F = sm.f[d];
+        const uint32_t* E = d < 2 ? sm.eyt : sm.ex;
+        const uint32_t* Vv = d < 2 ? sm.ezt : (d < 4 ? sm.ez : sm.ey);
+        const uint32_t fv = F[o];
+        uint32_t isow = 0;
+        if (fv) {
+          const uint32_t fu = v > 0 ? F[o - sv] : 0u;
+          const uint32_t fd = v < 31 ? F[o + sv] : 0u;
+          const uint32_t vd = v < 31 ? Vv[o + sv] : 0u;
+          const uint32_t left = fv & E[o] & (fv << 1);
+          const uint32_t upl = fv & Vv[o] & fu;
+          const uint32_t dnl = fv & vd & fd;
+          isow = fv & ~(left | (left >> 1) | upl | dnl);
         }
-        const uint64_t chunk_bits = (uint64_t)((p.chunk_id_base + (uint32_t)c) & 0xFFFFFu) << 44 |
-                                    (uint64_t)dir << 41;
-        uint64_t* qb = sm.qbuf[warp];
-        uint32_t mine = 0;
-        for (int v = 0; v < 32; v++) {
-          const int o = s * ss + v * sv;
-          uint32_t m = F[o];
-          const uint32_t e = E[o];
-          for (;;) {
-            if (qcnt > (uint32_t)(kQBuf - 32)) flush_quads(qb, qcnt, p, lane);
-            const bool have = m != 0;
-            const uint32_t act = __ballot_sync(kFull, have);
-            if (!act) break;
-            uint64_t q = 0;
-            if (have) {
-              const int u0 = __ffs(m) - 1;
-              const uint32_t run = (uint32_t)((uint64_t)(m & e) >> (u0 + 1));
-              const int w = __ffs(~run);  // 1..32
-              const uint32_t mask = (w == 32 ? kFull : ((1u << w) - 1u)) << u0;
-              int h = 1;
-              for (int r = v + 1; r < 32; r++) {
-                const int orow = s * ss + r * sv;
-                const uint32_t fr = F[orow];
-                if ((fr & V[orow] & mask) != mask) break;
-                F[orow] = fr & ~mask;
-                h++;
+        sm.iso[d][o] = isow;
+        // the 32 lanes of a warp share (d, v): one word group
+        const uint32_t n = __reduce_add_sync(kFull, (uint32_t)__popc(isow));
+        if (lane == 0) sm.iso_count[i >> 5] = n;
+      }
+      __syncthreads();
+      for (int i = tid; i < 6 * 1024; i += kThreads) {
+        const int d = i >> 10, v = (i >> 5) & 31, sl = i & 31;
+        const int o = word_off(d, sl, v);
+        sm.f[d][o] &= ~sm.iso[d][o];
+      }
+      if (warp == kWarps - 1) {
+        // exclusive prefix over the 192 word groups (6 per lane) and one
+        // reservation per chunk for all isolated quads
+        uint32_t cnt[6], sum = 0;
+        for (int k = 0; k < 6; k++) {
+          cnt[k] = sm.iso_count[lane * 6 + k];
+          sum += cnt[k];
+        }
+        uint32_t incl = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(kFull, incl, o);
+          if (lane >= o) incl += y;
+        }
+        uint32_t run = incl - sum;
+        for (int k = 0; k < 6; k++) {
+          sm.iso_off[lane * 6 + k] = run;
+          run += cnt[k];
+        }
+        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        if (lane == 0) {
+          sm.iso_base = total ? atomicAdd(p.count, (unsigned long long)total) : 0ull;
+          sm.chunk_quads += total;
+        }
+      }
+      __syncthreads();
+      // ---- pass 4: tasks 0-5 greedy on the remaining faces of direction t
+      // (lane = slice); tasks 6-17 bulk emission of isolated faces of
+      // direction (t-6)/2, rows 16*((t-6)%2) .. +16.
+      for (;;) {
+        int task = 0;
+        if (lane == 0) task = (int)atomicAdd(&sm.task_next, 1u);
+        task = __shfl_sync(kFull, task, 0);
+        if (task >= 6 + 48) break;
+        if (task < 6) {
+          const int dir = task, sl = lane;
+          uint32_t* F = sm.f[dir];
+          const uint32_t* E = dir < 2 ? sm.eyt : sm.ex;
+          const uint32_t* V = dir < 2 ? sm.ezt : (dir < 4 ? sm.ez : sm.ey);
+          const uint64_t chunk_bits = (uint64_t)((p.chunk_id_base + (uint32_t)c) & 0xFFFFFu) << 44 |
+                                      (uint64_t)dir << 41;
+          uint64_t* qb = sm.qbuf[dir];
+          uint32_t qc = sm.qcount[dir];
+          uint32_t mine = 0;
+          for (int v = 0; v < 32; v++) {
+            const int o = word_off(dir, sl, v);
+            uint32_t m = F[o];
+            const uint32_t e = E[o];
+            for (;;) {
+              if (qc > (uint32_t)(kQBuf - 32)) flush_quads(qb, qc, p, lane);
+              const bool have = m != 0;
+              const uint32_t act = __ballot_sync(kFull, have);
+              if (!act) break;
+              uint64_t q = 0;
+              if (have) {
+                const int u0 = __ffs(m) - 1;
+                const uint32_t run = __funnelshift_rc(m & e, 0u, (uint32_t)u0 + 1u);
+                const int w = __ffs(~run);  // 1..32
+                const uint32_t mask = ((2u << (w - 1)) - 1u) << u0;
+                int h = 1;
+                for (int r = v + 1; r < 32; r++) {
+                  const int orow = word_off(dir, sl, r);
+                  const uint32_t fr = F[orow];
+                  if ((fr & V[orow] & mask) != mask) break;
+                  F[orow] = fr & ~mask;
+                  h++;
+                }
+                m &= ~mask;
+                int x, y, z;
+                face_xyz(dir, sl, u0, v, x, y, z);
+                const uint32_t mat = load_mat<KIND>(mb, x, y, z);
+                q = chunk_bits | (uint64_t)z << 36 | (uint64_t)y << 31 | (uint64_t)x << 26 |
+                    (uint64_t)(w - 1) << 21 | (uint64_t)(h - 1) << 16 | (uint64_t)mat;
+                mine++;
               }
-              m &= ~mask;
-              int x, y, z;
-              if (dir < 2) { x = s; y = u0; z = v; }
-              else if (dir < 4) { x = u0; y = s; z = v; }
-              else { x = u0; y = v; z = s; }
-              const uint32_t mat = load_mat<KIND>(mb, x, y, z);
-              q = chunk_bits | (uint64_t)z << 36 | (uint64_t)y << 31 | (uint64_t)x << 26 |
-                  (uint64_t)(w - 1) << 21 | (uint64_t)(h - 1) << 16 | (uint64_t)mat;
-              mine++;
+              const uint32_t rank = __popc(act & lanemask_lt());
+              if (have) qb[qc + rank] = q;
+              qc += __popc(act);
             }
-            const uint32_t rank = __popc(act & lanemask_lt());
-            if (have) qb[qcnt + rank] = q;
-            qcnt += __popc(act);
           }
-        }
-        if (p.chunk_counts) {
-          const uint32_t tot = __reduce_add_sync(kFull, mine);
-          if (lane == 0) atomicAdd(&sm.chunk_quads, tot);
+          if (lane == 0) sm.qcount[dir] = qc;
+          if (p.chunk_counts) {
+            const uint32_t tot = __reduce_add_sync(kFull, mine);
+            if (lane == 0) atomicAdd(&sm.chunk_quads, tot);
+          }
+        } else {
+          // isolated faces of 4 word groups; per group a warp-balanced
+          // expansion: lane j of round k emits the (k*32+j)-th set bit of the
+          // group, found by a shuffle binary search over the lanes' prefixes
+          // and __fns inside the owning word
+          for (int g = (task - 6) * 4; g < (task - 6) * 4 + 4; g++) {
+            if (sm.iso_count[g] == 0) continue;
+            const int dir = g >> 5, v = g & 31;
+            const uint32_t wv = sm.iso[dir][word_off(dir, lane, v)];
+            const uint32_t cw = __popc(wv);
+            uint32_t incl = cw;
+            for (int o = 1; o < 32; o <<= 1) {
+              const uint32_t y = __shfl_up_sync(kFull, incl, o);
+              if (lane >= o) incl += y;
+            }
+            const uint32_t ex = incl - cw;
+            const uint32_t G = __shfl_sync(kFull, incl, 31);
+            const unsigned long long base = sm.iso_base + sm.iso_off[g];
+            const uint64_t dir_bits = (uint64_t)((p.chunk_id_base + (uint32_t)c) & 0xFFFFFu) << 44 |
+                                      (uint64_t)dir << 41;
+            for (uint32_t k = 0; k < G; k += 32) {
+              const uint32_t j = k + (uint32_t)lane;
+              int l = 0;
+#pragma unroll
+              for (int step = 16; step >= 1; step >>= 1) {
+                const uint32_t oc = __shfl_sync(kFull, ex, l + step);
+                if (oc <= j) l += step;
+              }
+              const uint32_t wl = __shfl_sync(kFull, wv, l);
+              const uint32_t ol = __shfl_sync(kFull, ex, l);
+              if (j < G) {
+                const int u = (int)__fns(wl, 0, (int)(j - ol) + 1);
+                int x, y, z;
+                face_xyz(dir, l, u, v, x, y, z);
+                const uint32_t mat = load_mat<KIND>(mb, x, y, z);
+                const uint64_t q = dir_bits | (uint64_t)z << 36 | (uint64_t)y << 31 | (uint64_t)x << 26 | mat;
+                const unsigned long long idx = base + j;
+                if (idx < p.cap) p.quads[idx] = q;
+              }
+            }
+          }
         }
       }
     }
     __syncthreads();
-    if (tid == 0 && p.chunk_counts) {
-      p.chunk_counts[c] = valid ? sm.chunk_quads : 0u;
+    if (tid == 0) {
+      if (p.chunk_counts) p.chunk_counts[c] = valid ? sm.chunk_quads : 0u;
       sm.chunk_quads = 0;
+      sm.task_next = 0;
     }
     buf ^= 1;
   }
-  if (warp < kGreedyWarps) flush_quads(sm.qbuf[warp], qcnt, p, lane);
+  if (warp < kGreedyWarps) {
+    uint32_t qc = sm.qcount[warp];
+    flush_quads(sm.qbuf[warp], qc, p, lane);
+  }
 }
 
 // --------------------------------------------------------------- host side
