@@ -65,6 +65,7 @@ struct __align__(128) MeshSmem {
   unsigned long long iso_base;       // global offset of the chunk's isolated quads
   uint32_t task_next;                // dynamic task counter of pass 4
   uint32_t qcount[kGreedyWarps];     // staged quads in qbuf[d]
+  uint32_t rest_rows[6];             // rows holding non-isolated faces, per direction
 };
 
 struct MeshParams {
@@ -336,6 +337,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   for (int i = tid; i < 6 * 32; i += kThreads) (&sm.halo[0][0])[i] = 0;
   if (tid < 192) sm.iso_count[tid] = 0;
   if (tid < kGreedyWarps) sm.qcount[tid] = 0;
+  if (tid < 6) sm.rest_rows[tid] = 0;
   if (tid == 0) sm.task_next = 0;
   __syncthreads();
   if (warp == 0) issue_chunk<KIND>(sm, p, &tmap, 0, lane, cur, end);
@@ -371,24 +373,37 @@ __global__ void __launch_bounds__(kThreads, 1)
       // lane y; Y faces by shuffles; X-face columns by warp transposes.
       for (int z = warp; z < 32; z += kWarps) {
         uint32_t r_occ = 0, r_ex = 0, r_ey = 0, r_ez = 0, prev_m = 0;
-#pragma unroll 4
-        for (int y = 0; y < 32; y++) {
-          const uint32_t m = load_mat<KIND>(mb, lane, y, z);
-          const uint32_t occw = __ballot_sync(kFull, m != 0);
-          if (lane == y) r_occ = occw;
-          if (occw) {  // equality bits only matter on solid voxels
-            const uint32_t mz = z > 0 ? load_mat<KIND>(mb, lane, y, z - 1) : 0u;
-            const uint32_t ml = __shfl_up_sync(kFull, m, 1);
-            const uint32_t exw = __ballot_sync(kFull, m == ml);
-            const uint32_t eyw = __ballot_sync(kFull, m == prev_m);
-            const uint32_t ezw = __ballot_sync(kFull, m == mz);
-            if (lane == y) {
-              r_ex = exw;
-              r_ey = eyw;
-              r_ez = ezw;
+        for (int y0 = 0; y0 < 32; y0 += 8) {
+          // 8 rows at a time: all loads first, then the votes
+          const int dl = lane - y0;  // row captured by this lane, if in 0..7
+          uint32_t m[8], occw[8];
+#pragma unroll
+          for (int k = 0; k < 8; k++) m[k] = load_mat<KIND>(mb, lane, y0 + k, z);
+          uint32_t any = 0;
+#pragma unroll
+          for (int k = 0; k < 8; k++) {
+            occw[k] = __ballot_sync(kFull, m[k] != 0);
+            any |= occw[k];
+            if (dl == k) r_occ = occw[k];
+          }
+          if (any) {  // equality bits only matter on solid voxels
+            uint32_t mz[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) mz[k] = z > 0 ? load_mat<KIND>(mb, lane, y0 + k, z - 1) : 0u;
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+              const uint32_t ml = __shfl_up_sync(kFull, m[k], 1);
+              const uint32_t exw = __ballot_sync(kFull, m[k] == ml);
+              const uint32_t eyw = __ballot_sync(kFull, m[k] == (k ? m[k - 1] : prev_m));
+              const uint32_t ezw = __ballot_sync(kFull, m[k] == mz[k]);
+              if (dl == k) {
+                r_ex = exw;
+                r_ey = eyw;
+                r_ez = ezw;
+              }
             }
           }
-          prev_m = m;
+          prev_m = m[7];
         }
         const int o = z * kS + lane;
         sm.occ[o] = r_occ;
@@ -427,6 +442,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       // ---- pass 3: isolated faces (no same-material face neighbour in the
       // plane).  Every greedy scan emits them as 1x1 quads and no other quad
       // touches them, so they are peeled off and emitted in bulk.
+#pragma unroll 4
       for (int i = tid; i < 6 * 1024; i += kThreads) {
         const int d = i >> 10, v = (i >> 5) & 31, sl = i & 31;
         const int o = word_off(d, sl, v), sv = d < 4 ? kS : 1;
@@ -453,7 +469,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int i = tid; i < 6 * 1024; i += kThreads) {
         const int d = i >> 10, v = (i >> 5) & 31, sl = i & 31;
         const int o = word_off(d, sl, v);
-        sm.f[d][o] &= ~sm.iso[d][o];
+        const uint32_t rest = sm.f[d][o] & ~sm.iso[d][o];
+        sm.f[d][o] = rest;
+        if (__any_sync(kFull, rest != 0) && lane == 0) atomicOr(&sm.rest_rows[d], 1u << v);
       }
       if (warp == kWarps - 1) {
         // exclusive prefix over the 192 word groups (6 per lane) and one
@@ -498,7 +516,10 @@ __global__ void __launch_bounds__(kThreads, 1)
           uint64_t* qb = sm.qbuf[dir];
           uint32_t qc = sm.qcount[dir];
           uint32_t mine = 0;
-          for (int v = 0; v < 32; v++) {
+          uint32_t rows = sm.rest_rows[dir];
+          while (rows) {
+            const int v = __ffs(rows) - 1;
+            rows &= rows - 1;
             const int o = word_off(dir, sl, v);
             uint32_t m = F[o];
             const uint32_t e = E[o];
@@ -534,7 +555,10 @@ __global__ void __launch_bounds__(kThreads, 1)
               qc += __popc(act);
             }
           }
-          if (lane == 0) sm.qcount[dir] = qc;
+          if (lane == 0) {
+            sm.qcount[dir] = qc;
+            sm.rest_rows[dir] = 0;
+          }
           if (p.chunk_counts) {
             const uint32_t tot = __reduce_add_sync(kFull, mine);
             if (lane == 0) atomicAdd(&sm.chunk_quads, tot);
