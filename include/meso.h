@@ -255,6 +255,23 @@ meso_status meso_raymarch_stats(meso_ctx* ctx, const meso_scene* const* scenes, 
                                 uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
                                 uint64_t h_counts[4]);
 
+/* Multi-view raymarch that allocates no memory.  No counterpart in the
+ * reference (it has no raymarcher); same launch and results as
+ * meso_raymarch.  For callers that cannot allocate device memory during the
+ * call -- a frame loop on a fixed device-memory budget that must not
+ * allocate mid-frame (an allocation can synchronise the device and stall the
+ * frame), or a host application whose own memory manager owns all device
+ * memory -- the view descriptors go to a fixed 64 KiB device array instead
+ * of a per-call allocation.  At most 512 views per call (more returns
+ * MESO_ERR_INVALID_ARG).  The array stays resident on every device that
+ * loads the library until the process exits.  The first call on a device
+ * looks up the array's address and caches it; make that first call before
+ * any stream capture.  All calls share the array: calls whose kernels
+ * overlap on the GPU race on it, so keep them on one stream or order them. */
+meso_status meso_raymarch_noalloc(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* h_cams,
+                                  uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
+                                  void* stream);
+
 /* ------------------------------------------------------------------- edits */
 
 typedef struct meso_sphere_edit {

@@ -507,3 +507,100 @@ meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, cons
 }
 
 }  // namespace meso
+
+// ---------------------------------------------------------------------------
+// Multi-view raymarch that allocates nothing.
+//
+// meso_raymarch stages the descriptor table of more than 32 views in device
+// memory it allocates per call.  Some callers cannot allocate device memory
+// at that point: a frame loop running on a fixed device-memory budget that
+// must not allocate mid-frame (an allocation can synchronise the device and
+// stall the frame), or a host application whose own memory manager owns all
+// device memory.  This entry point keeps the table in a fixed file-scope
+// device array instead, and stages the descriptors on the host stack.
+//
+// Limits and behaviour:
+//  - at most kNoAllocViews (512) views per call; more is rejected with
+//    MESO_ERR_INVALID_ARG;
+//  - the array (64 KiB) stays resident on every device that loads the
+//    library until the process exits;
+//  - the first call on a device looks up the array's device address (with
+//    that device current) and caches it; make that first call before any
+//    stream capture;
+//  - every call reuses the same array and overwrites the entries it uses, so
+//    calls whose kernels overlap on the GPU race on it: issue them on one
+//    stream, or order them with events.
+namespace meso {
+namespace {
+
+constexpr uint32_t kNoAllocViews = 512;
+static __device__ __align__(256) unsigned char g_noalloc_views[kNoAllocViews * sizeof(RayView)];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {};
+
+// Device address of g_noalloc_views on `device` (looked up once per device).
+meso_status noalloc_table(int device, void** out) {
+  if (device < 0 || device >= 64) return fail(MESO_ERR_INVALID_ARG, "raymarch_noalloc: device ordinal >= 64");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    int prev = 0;
+    MESO_CUDA_TRY(cudaGetDevice(&prev));
+    if (prev != device) MESO_CUDA_TRY(cudaSetDevice(device));
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_views);
+    if (prev != device) cudaSetDevice(prev);
+    if (e != cudaSuccess) return cuda_fail(e, "raymarch_noalloc: cudaGetSymbolAddress");
+    g_noalloc_ptr[device] = p;
+  }
+  *out = g_noalloc_ptr[device];
+  return MESO_OK;
+}
+
+}  // namespace
+}  // namespace meso
+
+extern "C" meso_status meso_raymarch_noalloc(meso_ctx* ctx, const meso_scene* const* scenes,
+                                             const meso_camera* h_cams, uint32_t n_views, const float light[3],
+                                             uint32_t flags, meso_hit* d_hits, void* stream) {
+  using namespace meso;
+  if (!ctx || !scenes || !h_cams || !d_hits) return fail(MESO_ERR_INVALID_ARG, "raymarch_noalloc: null argument");
+  if (n_views > kNoAllocViews)
+    return fail(MESO_ERR_INVALID_ARG, "raymarch_noalloc: at most 512 views per call (fixed device view table)");
+  if (n_views == 0) return MESO_OK;
+  for (uint32_t v = 0; v < n_views; v++) {
+    if (!scenes[v]) return fail(MESO_ERR_INVALID_ARG, "raymarch_noalloc: null scene");
+    if (h_cams[v].width == 0 || h_cams[v].height == 0 || h_cams[v].width > 16384 || h_cams[v].height > 16384)
+      return fail(MESO_ERR_INVALID_ARG, "raymarch_noalloc: image size out of range");
+  }
+  if ((flags & MESO_RAY_SHADOW) && !light) return fail(MESO_ERR_INVALID_ARG, "raymarch_noalloc: shadow without light");
+  const uint32_t tw = ctx->tuning.ray_tile_w ? ctx->tuning.ray_tile_w : 8;
+  if (32 % tw) return fail(MESO_ERR_INVALID_ARG, "raymarch_noalloc: tile width must divide 32");
+  const uint32_t th = 32 / tw;
+  const uint32_t wpc = ctx->tuning.ray_warps_per_cta ? ctx->tuning.ray_warps_per_cta : 4;
+  void* table = nullptr;
+  MESO_TRY(noalloc_table(ctx->device, &table));
+  RayView host[kNoAllocViews];
+  const uint64_t tiles = fill_views(scenes, h_cams, n_views, tw, th, host);
+  if (tiles >= (1ull << 31)) return fail(MESO_ERR_INVALID_ARG, "raymarch_noalloc: too many tiles");
+  RayParams P;
+  memset(&P, 0, sizeof(P));
+  P.table = static_cast<const RayView*>(table);
+  P.n_views = n_views;
+  P.total_tiles = (uint32_t)tiles;
+  P.tile_w = tw;
+  P.tile_h = th;
+  P.shadow = (flags & MESO_RAY_SHADOW) ? 1u : 0u;
+  if (light)
+    for (int a = 0; a < 3; a++) P.light[a] = light[a];
+  P.hits = d_hits;
+  const cudaStream_t st = pick_stream(ctx, stream);
+  // pageable source: the copy is staged before cudaMemcpyAsync returns
+  MESO_CUDA_TRY(cudaMemcpyAsync(table, host, sizeof(RayView) * (size_t)n_views, cudaMemcpyHostToDevice, st));
+  static InlineViews unused_inline;  // zero-initialised; the table path does not read it
+  const uint32_t blocks = (uint32_t)((tiles + wpc - 1) / wpc);
+  raymarch_kernel<false, false><<<blocks, wpc * 32, 0, st>>>(P, unused_inline);
+  ctx->launches.fetch_add(1);
+  MESO_CUDA_TRY(cudaGetLastError());
+  return MESO_OK;
+}
