@@ -145,6 +145,7 @@ def lib() -> ctypes.CDLL:
         "mo_mesh_chunks_mt": (u64, [P(Source), vp, u32, ctypes.c_int, vp, u64]),
         "mo_count_faces": (u64, [P(Source), vp]),
         "mo_camera_ray": (None, [P(Camera), u32, u32, vp]),
+        "mo_trace_ray": (None, [P(BrickMap), vp, vp, vp, vp, ctypes.c_int, vp]),
         "mo_raymarch_mt": (None, [P(BrickMap), P(Camera), u32, vp, ctypes.c_int, ctypes.c_int, vp]),
         "mo_raymarch_rows_mt": (None, [P(BrickMap), P(Camera), u32, u32, vp, ctypes.c_int, ctypes.c_int, vp]),
         "mo_edit_spheres": (ctypes.c_int, [P(BrickMap), P(Sphere), u32]),
@@ -379,6 +380,18 @@ def raymarch(bm: HostBrickMap, cams, light=None, shadow=True, nthreads=0) -> np.
     L = light_dir() if light is None else np.asarray(light, dtype=np.float32)
     lib().mo_raymarch_mt(ctypes.byref(bm.bm), arr, len(cams), _ptr(L), int(shadow), nthreads, _ptr(hits))
     return hits
+
+
+def trace_ray(bm: HostBrickMap, origin, direction, light=None, shadow=False):
+    """Traces one ray from a world-space origin (chunk-rebased internally)."""
+    o = np.asarray(origin, dtype=np.float64)
+    ch = np.floor(o / 32.0).astype(np.int32)
+    frac = (o - ch * 32.0).astype(np.float32)
+    d = np.asarray(direction, dtype=np.float32)
+    L = light_dir() if light is None else np.asarray(light, dtype=np.float32)
+    h = np.zeros(1, dtype=HIT_DTYPE)
+    lib().mo_trace_ray(ctypes.byref(bm.bm), _ptr(ch), _ptr(frac), _ptr(d), _ptr(L), int(shadow), _ptr(h))
+    return h[0]
 
 
 def raymarch_rows(bm: HostBrickMap, cam: Camera, row0: int, n_rows: int, light=None, shadow=True,

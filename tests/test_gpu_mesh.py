@@ -124,3 +124,15 @@ def test_brickmap_chunks(ctx):
     q, _ = ctx.mesh(meso.SRC_BRICKMAP, coords=coords, scene=scene)
     assert len(ref) > 0
     assert np.array_equal(_sorted(q), ref)
+
+
+def test_matches_golden_fixture(ctx):
+    import os
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    dev, _ = ctx.generate_chunks_u16(8, seed0=1)
+    q, _ = ctx.mesh(meso.SRC_CHUNKS_U16, dev, n=8)
+    assert np.array_equal(_sorted(q), np.load(os.path.join(golden, "quads_chunks_u16_seed1_n8.npy")))
+    g = ctx.generate_dense_u8(64, 64, 64, seed=1)
+    coords = np.array([(x, y, z) for z in range(2) for y in range(2) for x in range(2)], dtype=np.int32)
+    q2, _ = ctx.mesh(meso.SRC_GRID_U8, g, coords=coords, dims=(64, 64, 64))
+    assert np.array_equal(_sorted(q2), np.load(os.path.join(golden, "quads_dense_u8_64_seed1.npy")))

@@ -111,3 +111,12 @@ def test_raymarch_host_entry(ctx, small):
     cam = meso.camera((-20.0, 150.0, 90.0), (64.0, 64.0, 10.0), 64, 48)
     ocam = oracle.camera((-20.0, 150.0, 90.0), (64.0, 64.0, 10.0), 64, 48)
     assert_hits_equal(ctx.raymarch_host(scene, cam), oracle.raymarch(bm, ocam))
+
+
+def test_matches_golden_fixture(ctx, small):
+    import os
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    t, scene, bm = small
+    hits = ctx.raymarch(scene, meso.camera((-40.0, -30.0, 140.0), (64.0, 64.0, 20.0), 96, 64))
+    ref = np.load(os.path.join(golden, "hits_terrain128_96x64.npy"))
+    assert np.array_equal(hits.view(np.uint8), ref.view(np.uint8))
