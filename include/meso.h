@@ -326,6 +326,9 @@ typedef struct meso_server_config {
   uint64_t max_batch_rays;        /* primary rays per launch, 0 = 16M */
   uint64_t hbm_budget_bytes;      /* 0 = the context budget */
   uint32_t keep_hits;             /* 1 = copy hits back (meso_server_fetch_hits) */
+  uint32_t max_queue;             /* queued requests beyond this are rejected, 0 = no bound */
+  float light[3];                 /* direction towards the light (0,0,0 = normalize(0.3,0.5,0.8)) */
+  uint64_t max_edit_quads;        /* quad buffer of a remesh, 0 = 16M */
 } meso_server_config;
 
 /* The serving loop replaces the host ThreadPool + TDoubleBufferQueue pair

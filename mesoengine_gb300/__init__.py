@@ -114,6 +114,7 @@ class ServerConfig(ctypes.Structure):
     _fields_ = [
         ("max_inflight_batches", ctypes.c_uint32), ("max_batch_requests", ctypes.c_uint32),
         ("max_batch_rays", ctypes.c_uint64), ("hbm_budget_bytes", ctypes.c_uint64), ("keep_hits", ctypes.c_uint32),
+        ("max_queue", ctypes.c_uint32), ("light", ctypes.c_float * 3), ("max_edit_quads", ctypes.c_uint64),
     ]
 
 
@@ -584,3 +585,97 @@ def terrain_preset(name: str, seed: int | None = None) -> Terrain:
     }
     n, s, period, amp, base = presets[name]
     return Terrain(n, n, n, s if seed is None else seed, period, 6, base, amp, 48, 0.7)
+
+
+# ---------------------------------------------------------------- serving
+
+def hit_checksum(hits: np.ndarray) -> int:
+    """Host restatement of the server's order-sensitive hit hash:
+    sum_i mix64(w0 ^ mix64(w1 ^ mix64(w2 ^ (i*0x9E3779B97F4A7C15 + 1)))) mod 2^64,
+    w0..w2 the three 64-bit words of hit i, mix64 the splitmix64 finaliser."""
+    w = np.ascontiguousarray(hits).view(np.uint64).reshape(-1, 3)
+    i = np.arange(w.shape[0], dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        k = i * np.uint64(0x9E3779B97F4A7C15) + np.uint64(1)
+        h = _mix64(w[:, 0] ^ _mix64(w[:, 1] ^ _mix64(w[:, 2] ^ k)))
+        return int(np.sum(h, dtype=np.uint64))
+
+
+def quad_checksum(quads: np.ndarray) -> int:
+    """Order-insensitive quad hash: sum of mix64(q) mod 2^64."""
+    with np.errstate(over="ignore"):
+        return int(np.sum(_mix64(np.asarray(quads, dtype=np.uint64)), dtype=np.uint64))
+
+
+def _mix64(x):
+    x = np.asarray(x, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        x = x ^ (x >> np.uint64(30))
+        x = x * np.uint64(0xBF58476D1CE4E5B9)
+        x = x ^ (x >> np.uint64(27))
+        x = x * np.uint64(0x94D049BB133111EB)
+        x = x ^ (x >> np.uint64(31))
+    return x
+
+
+class Server:
+    """Continuous-batching request server over resident scenes."""
+
+    def __init__(self, ctx: Context, scenes, **cfg):
+        self.ctx = ctx
+        self.scenes = list(scenes)
+        c = ServerConfig()
+        for k, v in cfg.items():
+            if k == "light":
+                c.light[:] = list(v)
+            else:
+                setattr(c, k, v)
+        arr = (ctypes.c_void_p * len(self.scenes))(*[s.handle for s in self.scenes])
+        h = ctypes.c_void_p()
+        _check(_lib.meso_server_create(ctx.handle, ctypes.byref(c), arr, len(self.scenes), ctypes.byref(h)))
+        self.handle = h.value
+        self._keep = {}
+
+    def submit(self, scene_index: int, camera: Camera, shadow=False, edits=None, tag=0) -> int:
+        r = Request()
+        r.kind = REQ_EDIT_REMESH_RENDER if edits is not None else REQ_RENDER
+        r.scene_index = scene_index
+        r.camera = camera
+        r.flags = RAY_SHADOW if shadow else 0
+        arr = None
+        if edits:
+            arr = (SphereEdit * len(edits))(*edits)
+            r.n_edits = len(edits)
+            r.edits = ctypes.cast(arr, ctypes.POINTER(SphereEdit))
+        r.user_tag = tag
+        rid = ctypes.c_uint64()
+        _check(_lib.meso_server_submit(self.handle, ctypes.byref(r), ctypes.byref(rid)))
+        return int(rid.value)
+
+    def poll(self, max_n: int = 4096):
+        buf = (Completion * max_n)()
+        n = ctypes.c_uint32()
+        _check(_lib.meso_server_poll(self.handle, buf, max_n, ctypes.byref(n)))
+        return [buf[i] for i in range(n.value)]
+
+    def drain(self, timeout_s: float = 60.0) -> None:
+        _check(_lib.meso_server_drain(self.handle, timeout_s))
+
+    def now(self) -> float:
+        return float(_lib.meso_server_now(self.handle))
+
+    def fetch_hits(self, request_id: int, n: int) -> np.ndarray:
+        out = np.empty(n, dtype=HIT_DTYPE)
+        _check(_lib.meso_server_fetch_hits(self.handle, request_id, _np_ptr(out), n))
+        return out
+
+    def close(self) -> None:
+        if getattr(self, "handle", None) and _lib is not None:
+            _lib.meso_server_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

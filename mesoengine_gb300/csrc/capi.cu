@@ -115,6 +115,8 @@ meso_status meso_ctx_create(const meso_config* cfg, meso_ctx** out) {
   cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_scratch, 64);
   if (e == cudaSuccess) e = cudaMemset(ctx->d_scratch, 0, 64);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_tickets, 4 * meso_ctx::kTicketRing);
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_tickets, 0, 4 * meso_ctx::kTicketRing);
   if (e != cudaSuccess) {
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -129,6 +131,7 @@ void meso_ctx_destroy(meso_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   cudaFree(ctx->d_scratch);
+  cudaFree(ctx->d_tickets);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }

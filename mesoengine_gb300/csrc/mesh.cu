@@ -707,7 +707,7 @@ meso_status launch_mesh(meso_ctx* ctx, const meso_mesh_source* src, const int32_
   p.cap = out->capacity;
   p.count = reinterpret_cast<unsigned long long*>(out->d_quad_count);
   p.chunk_counts = out->d_chunk_quad_counts;
-  p.ticket = ctx->d_scratch + 0;
+  p.ticket = ctx->d_tickets + (ctx->next_ticket.fetch_add(1) % meso_ctx::kTicketRing);
   p.err = ctx->d_scratch + 1;
   p.per_ticket = ctx->tuning.mesh_chunks_per_ticket ? ctx->tuning.mesh_chunks_per_ticket : 1;
   CUtensorMap tmap;

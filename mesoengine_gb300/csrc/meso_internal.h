@@ -58,8 +58,14 @@ struct meso_ctx {
   uint64_t budget_bytes = 0;
   std::atomic<uint64_t> scene_bytes{0};
   std::atomic<uint64_t> launches{0};
-  // small device scratch: [0] mesh ticket, [1] error flags, [2..] spare
+  // small device scratch: [0] spare, [1] error flags, [2..63] spare
   uint32_t* d_scratch = nullptr;
+  // ring of queue tickets for persistent mesh launches; consecutive launches
+  // take consecutive counters, so up to kTicketRing launches may overlap on
+  // different streams
+  static constexpr uint32_t kTicketRing = 64;
+  uint32_t* d_tickets = nullptr;
+  std::atomic<uint32_t> next_ticket{0};
   std::mutex mu;
 };
 

@@ -1,0 +1,109 @@
+"""Serving loop: every result is the same alone and in the mix.
+
+Render requests of different sizes and scenes are batched into shared
+launches; edit+remesh+render requests are serialised per scene in arrival
+order.  Running the same request list one request at a time (submit, drain)
+and all at once must give identical per-request hit hashes, quad hashes and
+dirty-chunk counts; the kept hits equal a direct raymarch of the request.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import mesoengine_gb300 as meso
+
+pytestmark = pytest.mark.gpu
+
+
+def _scenes(ctx):
+    a = ctx.scene_from_terrain(meso.terrain_preset("small"), spare_bricks=4096)
+    b = ctx.scene_from_terrain(meso.Terrain(256, 256, 128, 21, 128, 6, 10.0, 48.0, 48, 0.7), spare_bricks=4096)
+    return [a, b]
+
+
+def _requests(seed, n=24, edits=True):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        sc = int(rng.integers(0, 2))
+        size = [(16, 16), (40, 24), (96, 64), (128, 72)][int(rng.integers(0, 4))]
+        o = (float(rng.uniform(-60, -10)), float(rng.uniform(-60, 60)), float(rng.uniform(90, 160)))
+        tg = (float(rng.uniform(40, 90)), float(rng.uniform(40, 90)), float(rng.uniform(0, 30)))
+        ed = None
+        if edits and rng.random() < 0.3:
+            ed = []
+            for _ in range(int(rng.integers(1, 6))):
+                c = (ctypes.c_int32 * 3)(*[int(v) for v in rng.integers(0, 120, 3)])
+                m = 0 if rng.random() < 0.5 else int(rng.integers(1, 65535))
+                ed.append(meso.SphereEdit(c, int(rng.integers(2, 12)), m, 0))
+        out.append((sc, meso.camera(o, tg, *size), bool(rng.random() < 0.5), ed))
+    return out
+
+
+def _run(ctx, reqs, one_by_one, keep_hits=False):
+    scenes = _scenes(ctx)
+    srv = meso.Server(ctx, scenes, max_inflight_batches=3, max_batch_rays=1 << 20, keep_hits=int(keep_hits),
+                      max_edit_quads=1 << 20)
+    res = {}
+    ids = []
+    for i, (sc, cam, shadow, ed) in enumerate(reqs):
+        ids.append(srv.submit(sc, cam, shadow=shadow, edits=ed, tag=i))
+        if one_by_one:
+            srv.drain()
+    srv.drain()
+    for c in srv.poll():
+        res[c.user_tag] = c
+    hits = {}
+    if keep_hits:
+        for i, rid in enumerate(ids):
+            cam = reqs[i][1]
+            hits[i] = srv.fetch_hits(rid, cam.width * cam.height)
+    srv.close()
+    return res, hits
+
+
+def test_render_results_equal_alone_and_in_mix(ctx):
+    reqs = _requests(1, edits=False)
+    alone, _ = _run(ctx, reqs, True)
+    mix, hits = _run(ctx, reqs, False, keep_hits=True)
+    scenes = _scenes(ctx)
+    for i, (sc, cam, shadow, _) in enumerate(reqs):
+        assert alone[i].status == 0 and mix[i].status == 0
+        assert alone[i].hit_checksum == mix[i].hit_checksum
+        direct = ctx.raymarch(scenes[sc], cam, shadow=shadow)
+        assert np.array_equal(hits[i].view(np.uint8), direct.view(np.uint8))
+        assert mix[i].hit_checksum == meso.hit_checksum(direct)
+        assert mix[i].n_rays == cam.width * cam.height + np.count_nonzero(direct["shadow_steps"])
+
+
+def test_edits_serialised_per_scene(ctx):
+    reqs = _requests(2)
+    assert any(r[3] for r in reqs)
+    alone, _ = _run(ctx, reqs, True)
+    mix, _ = _run(ctx, reqs, False)
+    for i, r in enumerate(reqs):
+        a, m = alone[i], mix[i]
+        assert a.status == 0 and m.status == 0, (a.status, m.status)
+        assert (a.hit_checksum, a.quad_checksum, a.n_quads, a.n_dirty_chunks) == \
+               (m.hit_checksum, m.quad_checksum, m.n_quads, m.n_dirty_chunks)
+        if r[3]:
+            assert m.n_dirty_chunks > 0
+
+
+def test_admission_rejects_oversize_and_overflowing_queue(ctx):
+    scenes = _scenes(ctx)
+    srv = meso.Server(ctx, scenes, max_inflight_batches=1, max_batch_requests=1, max_batch_rays=64 * 64,
+                      max_queue=2)
+    big = srv.submit(0, meso.camera((-40.0, -30.0, 140.0), (64.0, 64.0, 20.0), 128, 128))
+    cam = meso.camera((-40.0, -30.0, 140.0), (64.0, 64.0, 20.0), 64, 64)
+    ids = [srv.submit(0, cam, shadow=True) for _ in range(400)]
+    srv.drain()
+    comp = {c.request_id: c for c in srv.poll()}
+    srv.close()
+    assert comp[big].status == 3  # MESO_ERR_OVER_BUDGET: can never fit a slot
+    st = [comp[i].status for i in ids]
+    assert st.count(0) >= 2 and st.count(3) >= 1 and set(st) <= {0, 3}
+    for i in ids:
+        c = comp[i]
+        assert c.done_s >= c.submit_s
