@@ -241,6 +241,135 @@ def bench_mesh(ctx, meso, steps, warmup):
             "gvox_s_plain": vox / (ms_plain * 1e6), "algo_bytes": algo}
 
 
+def poisson_arrivals(rate, seconds, seed):
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > seconds:
+            return out
+        out.append(t)
+
+
+def outside_pose(rng, n, target):
+    """Camera origin outside the n^3 grid (distance 1.1 n from the centre, upper hemisphere)."""
+    v = rng.normal(size=3)
+    v[2] = abs(v[2]) + 0.2
+    v /= np.linalg.norm(v)
+    return tuple(float(c) for c in (np.full(3, n / 2.0) + v * 1.1 * n)), tuple(float(c) for c in target)
+
+
+def replay(server, items, submit):
+    """Submits items[k] = (arrival_s, ...) at their arrival times; returns completions."""
+    comps = []
+    t0 = server.now()
+    i = 0
+    while i < len(items):
+        now = server.now() - t0
+        while i < len(items) and items[i][0] <= now:
+            submit(items[i])
+            i += 1
+        comps += server.poll()
+        if i < len(items):
+            dt = items[i][0] - (server.now() - t0)
+            if dt > 2e-4:
+                time.sleep(min(dt, 1e-3))
+    server.drain(600.0)
+    comps += server.poll()
+    return comps
+
+
+def summarize(comps):
+    ok = [c for c in comps if c.status == 0]
+    lat = np.array([c.done_s - c.submit_s for c in ok]) * 1e3
+    span = (max(c.done_s for c in ok) - min(c.submit_s for c in comps)) if ok else 1.0
+    rays = sum(c.n_rays for c in ok)
+    return {
+        "requests": len(comps), "completed": len(ok), "rejected": sum(c.status == 3 for c in comps),
+        "p50_ms": round(float(np.percentile(lat, 50)), 3) if len(lat) else None,
+        "p99_ms": round(float(np.percentile(lat, 99)), 3) if len(lat) else None,
+        "mrays_s": round(rays / span / 1e6, 1), "span_s": round(span, 3),
+    }
+
+
+def bench_serve_render(ctx, meso, seconds, rate=2000.0):
+    """Served raymarching: 4 resident scenes (512^3, 1024^3, 1024^3, 2048^3),
+    Poisson arrivals, image size uniform over {256^2, 512^2, 1920x1080,
+    3840x2160}, primary rays only, 120 GB HBM budget."""
+    names = ("serve512", "serve1024", "serve1024b", "serve2048")
+    scenes = [ctx.scene_from_terrain(meso.terrain_preset(n)) for n in names]
+    dims = [meso.terrain_preset(n).nx for n in names]
+    sizes = [(256, 256), (512, 512), (1920, 1080), (3840, 2160)]
+    rng = np.random.default_rng(7)
+    items = []
+    for t in poisson_arrivals(rate, seconds, 7):
+        s = int(rng.integers(0, 4))
+        n = dims[s]
+        tgt = (rng.uniform(0.25, 0.75) * n, rng.uniform(0.25, 0.75) * n, rng.uniform(0.02, 0.2) * n)
+        o, tg = outside_pose(rng, n, tgt)
+        w, h = sizes[int(rng.integers(0, 4))]
+        items.append((t, s, meso.camera(o, tg, w, h)))
+    srv = meso.Server(ctx, scenes, max_inflight_batches=4, max_batch_rays=16 << 20, max_queue=512,
+                      hbm_budget_bytes=120 << 30)
+    comps = replay(srv, items, lambda it: srv.submit(it[1], it[2], shadow=False))
+    srv.close()
+    res = summarize(comps)
+    res["offered_mrays_s"] = round(sum(it[2].width * it[2].height for it in items) / seconds / 1e6, 1)
+    # plain form: one launch per request, waited for one at a time
+    k = min(300, len(items))
+    ctx.sync()
+    t0 = time.perf_counter()
+    px = 0
+    for it in items[:k]:
+        out = ctx.raymarch(scenes[it[1]], it[2], shadow=False, download=False)
+        ctx.sync()
+        px += it[2].width * it[2].height
+        out.free()
+    res["plain_per_view_mrays_s"] = round(px / (time.perf_counter() - t0) / 1e6, 1)
+    res["served_over_plain"] = round(res["mrays_s"] / max(res["plain_per_view_mrays_s"], 1e-9), 2)
+    res["workload"] = (f"4 resident scenes {dims}, Poisson {rate:.0f} req/s for {seconds:.0f} s (seed 7), "
+                       "sizes {256^2, 512^2, 1920x1080, 3840x2160}, primary rays, HBM budget 120 GB")
+    for s in scenes:
+        s.destroy()
+    return res
+
+
+def bench_serve_edit(ctx, meso, seconds, rate=200.0):
+    """Served edit + remesh + render on the 4096^3 scene (~2% solid): 1-32
+    spheres per request (radius 2-32, add/remove 50/50, material 1..65535),
+    remesh of the dirty 32^3 chunks, then a 1920x1080 render (primary)."""
+    t = meso.terrain_preset("edit4096")
+    scene = ctx.scene_from_terrain(t, spare_bricks=4 << 20)
+    n = t.nx
+    rng = np.random.default_rng(9)
+    items = []
+    for ta in poisson_arrivals(rate, seconds, 9):
+        edits = []
+        for _ in range(int(rng.integers(1, 33))):
+            c = [int(rng.integers(0, n)), int(rng.integers(0, n)), int(rng.integers(0, 192))]
+            m = 0 if rng.random() < 0.5 else int(rng.integers(1, 65536))
+            import ctypes
+            edits.append(meso.SphereEdit((ctypes.c_int32 * 3)(*c), int(rng.integers(2, 33)), m, 0))
+        o, tg = outside_pose(rng, n, (edits[0].center[0], edits[0].center[1], edits[0].center[2]))
+        items.append((ta, edits, meso.camera(o, tg, 1920, 1080)))
+    srv = meso.Server(ctx, [scene], max_inflight_batches=4, max_batch_rays=4 << 20, max_queue=512,
+                      max_edit_quads=64 << 20)
+    comps = replay(srv, items, lambda it: srv.submit(0, it[2], shadow=False, edits=it[1]))
+    srv.close()
+    res = summarize(comps)
+    ok = [c for c in comps if c.status == 0]
+    chunks = sum(c.n_dirty_chunks for c in ok)
+    busy = sum(c.done_s - c.start_s for c in ok)
+    res["dirty_chunks"] = chunks
+    res["quads"] = int(sum(c.n_quads for c in ok))
+    res["gvox_meshed_s_wall"] = round(chunks * 32768 / res["span_s"] / 1e9, 3)
+    res["gvox_meshed_s_busy"] = round(chunks * 32768 / max(busy, 1e-9) / 1e9, 3)
+    res["workload"] = (f"4096^3 terrain (512^3 pointer grid), Poisson {rate:.0f} req/s for {seconds:.0f} s (seed 9), "
+                       "1-32 sphere edits + remesh of dirty chunks + 1920x1080 primary render")
+    scene.destroy()
+    return res
+
+
 def cpu_baseline_port(meso, ctx, r):
     """Oracle DDA on the host cores over the whole frame, scene copied from the device."""
     import oracle
@@ -315,6 +444,9 @@ def run_ours(args, world, rank, local, dist):
                          "frac": round(ach / hbm, 4), "algorithmic_bytes_per_launch": m["algo_bytes"],
                          "kernel": "mesh_kernel<CHUNKS_U16>"},
         }
+    if rank == 0 and not args.skip_serve:
+        line["served"] = bench_serve_render(ctx, meso, args.serve_seconds)
+        line["served_edit"] = bench_serve_edit(ctx, meso, args.serve_seconds)
     if rank == 0 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline_port(meso, ctx, r)
     if rank == 0:
@@ -395,6 +527,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-mesh", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-serve", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.profile:
         run_profile_case(args.profile)

@@ -346,6 +346,21 @@ meso_status meso_server_drain(meso_server* srv, double timeout_s);
 double meso_server_now(const meso_server* srv);
 meso_status meso_server_destroy(meso_server* srv);
 
+/* ------------------------------------------------------------------ graphs */
+
+/* CUDA-graph capture of a sequence of stream-ordered meso calls (meshing,
+ * raymarching, memset/copy helpers) issued on `stream` between begin and end;
+ * meso_graph_launch replays it with one launch.  Calls that wait for the
+ * device (meso_sync, meso_mesh_check, scene creation, edits, the host-buffer
+ * forms) must not be issued while capturing.  A captured mesh launch keeps
+ * the queue ticket it was given; replays of one graph must not overlap each
+ * other on different streams. */
+typedef struct meso_graph meso_graph;
+meso_status meso_capture_begin(meso_ctx* ctx, void* stream);
+meso_status meso_capture_end(meso_ctx* ctx, void* stream, meso_graph** out);
+meso_status meso_graph_launch(meso_graph* graph, void* stream);
+meso_status meso_graph_destroy(meso_graph* graph);
+
 /* ------------------------------------------------------------------ tuning */
 
 /* Grid search over mesher CTAs per SM and chunks per ticket, and ray tile

@@ -181,6 +181,12 @@ _SIGNATURES = {
     "meso_server_drain": [ctypes.c_void_p, ctypes.c_double],
     "meso_server_destroy": [ctypes.c_void_p],
     "meso_autotune": [ctypes.c_void_p, ctypes.c_char_p],
+    "meso_capture_begin": [ctypes.c_void_p, ctypes.c_void_p],
+    "meso_capture_end": [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)],
+    "meso_graph_launch": [ctypes.c_void_p, ctypes.c_void_p],
+    "meso_graph_destroy": [ctypes.c_void_p],
+    "meso_raymarch_noalloc": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Camera),
+                              ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p],
 }
 
 
@@ -531,6 +537,18 @@ class Context:
     def pinned(self, nbytes: int) -> PinnedBuffer:
         return PinnedBuffer(self, nbytes)
 
+    def capture(self, fn, stream):
+        """Captures the stream-ordered calls fn() issues on `stream` into a
+        CUDA graph; returns a Graph whose launch() replays them."""
+        _check(_lib.meso_capture_begin(self.handle, stream))
+        try:
+            fn()
+        finally:
+            g = ctypes.c_void_p()
+            rc = _lib.meso_capture_end(self.handle, stream, ctypes.byref(g))
+        _check(rc)
+        return Graph(g.value)
+
     def autotune(self, path: str | None = None) -> None:
         _check(_lib.meso_autotune(self.handle, path.encode() if path else None))
 
@@ -538,6 +556,25 @@ class Context:
         if getattr(self, "handle", None) and _lib is not None:
             _lib.meso_ctx_destroy(self.handle)
         self.handle = None
+
+
+class Graph:
+    def __init__(self, handle):
+        self.handle = handle
+
+    def launch(self, stream=None) -> None:
+        _check(_lib.meso_graph_launch(self.handle, stream))
+
+    def destroy(self) -> None:
+        if self.handle and _lib is not None:
+            _lib.meso_graph_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------- helpers

@@ -445,4 +445,48 @@ meso_status meso_edit_spheres(meso_ctx* ctx, meso_scene* scene, const meso_spher
   return edit_spheres(ctx, scene, h_spheres, n, h_dirty, dirty_cap, n_dirty, pick_stream(ctx, stream));
 }
 
+// ------------------------------------------------------------------ graphs
+
+struct meso_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+meso_status meso_capture_begin(meso_ctx* ctx, void* stream) {
+  if (!ctx || !stream) return fail(MESO_ERR_INVALID_ARG, "capture_begin: needs a context and an explicit stream");
+  MESO_CUDA_TRY(cudaStreamBeginCapture((cudaStream_t)stream, cudaStreamCaptureModeThreadLocal));
+  return MESO_OK;
+}
+
+meso_status meso_capture_end(meso_ctx* ctx, void* stream, meso_graph** out) {
+  if (!ctx || !stream || !out) return fail(MESO_ERR_INVALID_ARG, "capture_end: null argument");
+  cudaGraph_t g = nullptr;
+  MESO_CUDA_TRY(cudaStreamEndCapture((cudaStream_t)stream, &g));
+  cudaGraphExec_t x = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&x, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return cuda_fail(e, "capture_end: cudaGraphInstantiate");
+  }
+  meso_graph* mg = new meso_graph();
+  mg->graph = g;
+  mg->exec = x;
+  *out = mg;
+  return MESO_OK;
+}
+
+meso_status meso_graph_launch(meso_graph* graph, void* stream) {
+  if (!graph) return fail(MESO_ERR_INVALID_ARG, "graph_launch: null graph");
+  MESO_CUDA_TRY(cudaGraphLaunch(graph->exec, (cudaStream_t)stream));
+  return MESO_OK;
+}
+
+meso_status meso_graph_destroy(meso_graph* graph) {
+  if (!graph) return MESO_OK;
+  if (graph->exec) cudaGraphExecDestroy(graph->exec);
+  if (graph->graph) cudaGraphDestroy(graph->graph);
+  delete graph;
+  return MESO_OK;
+}
+
 }  // extern "C"
