@@ -87,3 +87,11 @@ def test_product_does_not_use_the_oracle():
             if f.endswith((".cu", ".h", ".cpp", ".py")):
                 text = open(os.path.join(d, f)).read()
                 assert "meso_oracle" not in text and "import oracle" not in text, f
+
+
+def test_cpp_wrapper_header_compiles():
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "w.cpp")
+        open(c, "w").write('#include "meso.hpp"\nint main() { return 0; }\n')
+        subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-I", os.path.join(ROOT, "include"), c],
+                       check=True)
