@@ -37,10 +37,9 @@ using namespace ::meso::dev;
 
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
-constexpr int kGreedyWarps = 6;
 constexpr int kS = 33;               // padded row stride of 32x32 word arrays
 constexpr int kArr = 32 * kS;
-constexpr int kQBuf = 256;           // staged quads per greedy warp
+constexpr int kQBuf = 256;           // staged quads per warp
 constexpr int kBrickSlot = 1040;     // bytes per staged brick (bank-spread padding)
 constexpr int kMatBuf = 64 * kBrickSlot;
 constexpr uint32_t kFull = 0xFFFFFFFFu;
@@ -52,9 +51,9 @@ struct __align__(128) MeshSmem {
   uint32_t ex[kArr], ey[kArr], ez[kArr];  // equality with -x / -y / -z neighbour, bits over x, [z][y]
   uint32_t eyt[kArr], ezt[kArr];          // equality with -y / -z neighbour, bits over y, [z][x]
   uint32_t f[6][kArr];                    // face masks; X: [z][x] bits y; Y,Z: [z][y] bits x
-  uint32_t iso[6][kArr];                  // faces linked to no same-material face: 1x1 quads
   uint32_t halo[6][32];                   // -X,+X: bits y by z; -Y,+Y: bits x by z; -Z,+Z: bits x by y
-  uint64_t qbuf[kGreedyWarps][kQBuf];
+  uint64_t qbuf[kWarps][kQBuf];           // staged greedy quads per warp
+  uint32_t rest_rows[192];                // per slice 32*dir + s: rows holding non-isolated faces
   uint64_t bar[2];
   int32_t chunk[2];
   int32_t valid[2];
@@ -64,8 +63,7 @@ struct __align__(128) MeshSmem {
   uint32_t iso_off[192];             // their exclusive prefix within the chunk
   unsigned long long iso_base;       // global offset of the chunk's isolated quads
   uint32_t task_next;                // dynamic task counter of pass 4
-  uint32_t qcount[kGreedyWarps];     // staged quads in qbuf[d]
-  uint32_t rest_rows[6];             // rows holding non-isolated faces, per direction
+  uint32_t qcnt[kWarps];             // staged quads in qbuf[warp]
 };
 
 struct MeshParams {
@@ -279,19 +277,6 @@ __device__ __forceinline__ void compute_halos(MeshSmem& sm, const MeshParams& p,
   }
 }
 
-__device__ __forceinline__ void flush_quads(uint64_t* qb, uint32_t& cnt, const MeshParams& p, int lane) {
-  __syncwarp();
-  unsigned long long base = 0;
-  if (lane == 0 && cnt) base = atomicAdd(p.count, (unsigned long long)cnt);
-  base = __shfl_sync(kFull, base, 0);
-  for (uint32_t i = lane; i < cnt; i += 32) {
-    const unsigned long long idx = base + i;
-    if (idx < p.cap) p.quads[idx] = qb[i];
-  }
-  __syncwarp();
-  cnt = 0;
-}
-
 // In-register 32x32 bit transpose across a warp: lane r holds row r (bit c =
 // element (r, c)); afterwards lane c holds column c (bit r).  Five butterfly
 // stages swap the off-diagonal blocks of size 16, 8, 4, 2, 1.
@@ -316,6 +301,22 @@ __device__ __forceinline__ void face_xyz(int d, int s, int u, int v, int& x, int
   else { x = u; y = v; z = s; }
 }
 
+// Appends the warp's staged quads to the output (one atomic per flush).
+__device__ __forceinline__ void flush_warp(MeshSmem& sm, int warp, const MeshParams& p, int lane) {
+  __syncwarp();
+  const uint32_t cnt = sm.qcnt[warp];
+  unsigned long long base = 0;
+  if (lane == 0 && cnt) base = atomicAdd(p.count, (unsigned long long)cnt);
+  base = __shfl_sync(kFull, base, 0);
+  for (uint32_t i = lane; i < cnt; i += 32) {
+    const unsigned long long idx = base + i;
+    if (idx < p.cap) p.quads[idx] = sm.qbuf[warp][i];
+  }
+  __syncwarp();
+  if (lane == 0) sm.qcnt[warp] = 0;
+  __syncwarp();
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(kThreads, 1)
     mesh_kernel(const MeshParams p, const __grid_constant__ CUtensorMap tmap) {
@@ -336,8 +337,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   for (int i = tid; i < 6 * 32; i += kThreads) (&sm.halo[0][0])[i] = 0;
   if (tid < 192) sm.iso_count[tid] = 0;
-  if (tid < kGreedyWarps) sm.qcount[tid] = 0;
-  if (tid < 6) sm.rest_rows[tid] = 0;
+  if (tid < 192) sm.rest_rows[tid] = 0;
+  if (tid < kWarps) sm.qcnt[tid] = 0;
   if (tid == 0) sm.task_next = 0;
   __syncthreads();
   if (warp == 0) issue_chunk<KIND>(sm, p, &tmap, 0, lane, cur, end);
@@ -441,16 +442,20 @@ __global__ void __launch_bounds__(kThreads, 1)
       __syncthreads();
       // ---- pass 3: isolated faces (no same-material face neighbour in the
       // plane).  Every greedy scan emits them as 1x1 quads and no other quad
-      // touches them, so they are peeled off and emitted in bulk.
-#pragma unroll 4
-      for (int i = tid; i < 6 * 1024; i += kThreads) {
+      // touches them, so they are peeled off into registers (thread t holds
+      // the words i = t + 512k, k < 12; a warp holds whole 32-word groups
+      // g = 32*dir + row) and emitted in bulk.
+      uint32_t isow[12];
+#pragma unroll
+      for (int k = 0; k < 12; k++) {
+        const int i = tid + k * kThreads;
         const int d = i >> 10, v = (i >> 5) & 31, sl = i & 31;
         const int o = word_off(d, sl, v), sv = d < 4 ? kS : 1;
         const uint32_t* F = sm.f[d];
         const uint32_t* E = d < 2 ? sm.eyt : sm.ex;
         const uint32_t* Vv = d < 2 ? sm.ezt : (d < 4 ? sm.ez : sm.ey);
         const uint32_t fv = F[o];
-        uint32_t isow = 0;
+        uint32_t w = 0;
         if (fv) {
           const uint32_t fu = v > 0 ? F[o - sv] : 0u;
           const uint32_t fd = v < 31 ? F[o + sv] : 0u;
@@ -458,20 +463,21 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t left = fv & E[o] & (fv << 1);
           const uint32_t upl = fv & Vv[o] & fu;
           const uint32_t dnl = fv & vd & fd;
-          isow = fv & ~(left | (left >> 1) | upl | dnl);
+          w = fv & ~(left | (left >> 1) | upl | dnl);
         }
-        sm.iso[d][o] = isow;
-        // the 32 lanes of a warp share (d, v): one word group
-        const uint32_t n = __reduce_add_sync(kFull, (uint32_t)__popc(isow));
+        isow[k] = w;
+        const uint32_t n = __reduce_add_sync(kFull, (uint32_t)__popc(w));
         if (lane == 0) sm.iso_count[i >> 5] = n;
       }
       __syncthreads();
-      for (int i = tid; i < 6 * 1024; i += kThreads) {
+#pragma unroll
+      for (int k = 0; k < 12; k++) {
+        const int i = tid + k * kThreads;
         const int d = i >> 10, v = (i >> 5) & 31, sl = i & 31;
         const int o = word_off(d, sl, v);
-        const uint32_t rest = sm.f[d][o] & ~sm.iso[d][o];
+        const uint32_t rest = sm.f[d][o] & ~isow[k];
         sm.f[d][o] = rest;
-        if (__any_sync(kFull, rest != 0) && lane == 0) atomicOr(&sm.rest_rows[d], 1u << v);
+        if (rest) atomicOr(&sm.rest_rows[d * 32 + sl], 1u << v);
       }
       if (warp == kWarps - 1) {
         // exclusive prefix over the 192 word groups (6 per lane) and one
@@ -498,114 +504,115 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       __syncthreads();
-      // ---- pass 4: tasks 0-5 greedy on the remaining faces of direction t
-      // (lane = slice); tasks 6-17 bulk emission of isolated faces of
-      // direction (t-6)/2, rows 16*((t-6)%2) .. +16.
+      const uint64_t chunk_bits = (uint64_t)((p.chunk_id_base + (uint32_t)c) & 0xFFFFFu) << 44;
+      // ---- pass 4a: isolated quads of this warp's 12 groups; per group a
+      // warp-balanced expansion: lane j of round k emits the (32k+j)-th set
+      // bit of the group, found by a shuffle binary search over the lanes'
+      // prefixes and __fns inside the owning word
+#pragma unroll
+      for (int k = 0; k < 12; k++) {
+        const int g = warp + k * kWarps;
+        if (sm.iso_count[g] == 0) continue;
+        const int dir = g >> 5, v = g & 31;
+        const uint32_t wv = isow[k];
+        const uint32_t cw = __popc(wv);
+        uint32_t incl = cw;
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(kFull, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const uint32_t ex = incl - cw;
+        const uint32_t G = __shfl_sync(kFull, incl, 31);
+        const unsigned long long base = sm.iso_base + sm.iso_off[g];
+        const uint64_t dir_bits = chunk_bits | (uint64_t)dir << 41;
+        for (uint32_t k2 = 0; k2 < G; k2 += 32) {
+          const uint32_t j = k2 + (uint32_t)lane;
+          int l = 0;
+#pragma unroll
+          for (int step = 16; step >= 1; step >>= 1) {
+            const uint32_t oc = __shfl_sync(kFull, ex, l + step);
+            if (oc <= j) l += step;
+          }
+          const uint32_t wl = __shfl_sync(kFull, wv, l);
+          const uint32_t ol = __shfl_sync(kFull, ex, l);
+          if (j < G) {
+            const int u = (int)__fns(wl, 0, (int)(j - ol) + 1);
+            int x, y, z;
+            face_xyz(dir, l, u, v, x, y, z);
+            const uint32_t mat = load_mat<KIND>(mb, x, y, z);
+            const uint64_t q = dir_bits | (uint64_t)z << 36 | (uint64_t)y << 31 | (uint64_t)x << 26 | mat;
+            const unsigned long long idx = base + j;
+            if (idx < p.cap) p.quads[idx] = q;
+          }
+        }
+      }
+      // ---- pass 4b: greedy on the remaining faces, one warp per slice.
+      // Lane r holds row r of the slice in registers: its faces, their
+      // equality with the -u and -v neighbours, and the bits consumed so far.  Rows are scanned in
+      // order; in a row every maximal run of unconsumed same-material faces
+      // is one quad (Lysenko's left-to-right scan gives exactly these runs);
+      // a quad's height is one ballot over the rows below, and the quads of
+      // one row never interact because their columns are disjoint.
+      uint64_t* qb = sm.qbuf[warp];
+      uint32_t mine = 0;
       for (;;) {
         int task = 0;
         if (lane == 0) task = (int)atomicAdd(&sm.task_next, 1u);
         task = __shfl_sync(kFull, task, 0);
-        if (task >= 6 + 48) break;
-        if (task < 6) {
-          const int dir = task, sl = lane;
-          uint32_t* F = sm.f[dir];
-          const uint32_t* E = dir < 2 ? sm.eyt : sm.ex;
-          const uint32_t* V = dir < 2 ? sm.ezt : (dir < 4 ? sm.ez : sm.ey);
-          const uint64_t chunk_bits = (uint64_t)((p.chunk_id_base + (uint32_t)c) & 0xFFFFFu) << 44 |
-                                      (uint64_t)dir << 41;
-          uint64_t* qb = sm.qbuf[dir];
-          uint32_t qc = sm.qcount[dir];
-          uint32_t mine = 0;
-          uint32_t rows = sm.rest_rows[dir];
-          while (rows) {
-            const int v = __ffs(rows) - 1;
-            rows &= rows - 1;
-            const int o = word_off(dir, sl, v);
-            uint32_t m = F[o];
-            const uint32_t e = E[o];
-            for (;;) {
-              if (qc > (uint32_t)(kQBuf - 32)) flush_quads(qb, qc, p, lane);
-              const bool have = m != 0;
-              const uint32_t act = __ballot_sync(kFull, have);
-              if (!act) break;
-              uint64_t q = 0;
-              if (have) {
-                const int u0 = __ffs(m) - 1;
-                const uint32_t run = __funnelshift_rc(m & e, 0u, (uint32_t)u0 + 1u);
-                const int w = __ffs(~run);  // 1..32
-                const uint32_t mask = ((2u << (w - 1)) - 1u) << u0;
-                int h = 1;
-                for (int r = v + 1; r < 32; r++) {
-                  const int orow = word_off(dir, sl, r);
-                  const uint32_t fr = F[orow];
-                  if ((fr & V[orow] & mask) != mask) break;
-                  F[orow] = fr & ~mask;
-                  h++;
-                }
-                m &= ~mask;
-                int x, y, z;
-                face_xyz(dir, sl, u0, v, x, y, z);
-                const uint32_t mat = load_mat<KIND>(mb, x, y, z);
-                q = chunk_bits | (uint64_t)z << 36 | (uint64_t)y << 31 | (uint64_t)x << 26 |
-                    (uint64_t)(w - 1) << 21 | (uint64_t)(h - 1) << 16 | (uint64_t)mat;
-                mine++;
-              }
-              const uint32_t rank = __popc(act & lanemask_lt());
-              if (have) qb[qc + rank] = q;
-              qc += __popc(act);
-            }
+        if (task >= 192) break;
+        uint32_t rows = sm.rest_rows[task];
+        if (!rows) continue;
+        if (lane == 0) sm.rest_rows[task] = 0;
+        const int dir = task >> 5, sl = task & 31;
+        const int orow = word_off(dir, sl, lane);
+        const uint32_t Fr = sm.f[dir][orow];
+        const uint32_t Er = (dir < 2 ? sm.eyt : sm.ex)[orow];
+        const uint32_t Vr = (dir < 2 ? sm.ezt : (dir < 4 ? sm.ez : sm.ey))[orow];
+        const uint64_t dir_bits = chunk_bits | (uint64_t)dir << 41;
+        uint32_t cons = 0;
+        while (rows) {
+          const int v = __ffs(rows) - 1;
+          rows &= rows - 1;
+          const uint32_t cur = Fr & ~cons;
+          const uint32_t word = __shfl_sync(kFull, cur, v);
+          if (!word) continue;
+          const uint32_t e = __shfl_sync(kFull, Er, v);
+          const uint32_t link = word & e & (word << 1);
+          const uint32_t starts = word & ~link;
+          const uint32_t cnt = __popc(starts);
+          if (sm.qcnt[warp] + cnt > (uint32_t)kQBuf) flush_warp(sm, warp, p, lane);
+          const uint32_t q0 = sm.qcnt[warp];
+          // every start lane grows its quad; row r's words come from lane r
+          const bool is_start = (starts >> lane) & 1u;
+          const int w = __ffs(~__funnelshift_rc(link, 0u, (uint32_t)lane + 1u));
+          const uint32_t mask = is_start ? ((2u << (w - 1)) - 1u) << lane : 0u;
+          const uint32_t grow = Fr & Vr;  // faces that continue the row above in material
+          bool active = is_start;
+          int h = 1;
+          for (int r = v + 1; r < 32; r++) {
+            const uint32_t g = __shfl_sync(kFull, grow & ~cons, r);
+            const bool cont = active && (g & mask) == mask;
+            const uint32_t taken = __reduce_or_sync(kFull, cont ? mask : 0u);
+            if (lane == r) cons |= taken;
+            h += cont ? 1 : 0;
+            active = cont;
+            if (!__any_sync(kFull, active)) break;
           }
-          if (lane == 0) {
-            sm.qcount[dir] = qc;
-            sm.rest_rows[dir] = 0;
+          if (is_start) {
+            int x, y, z;
+            face_xyz(dir, sl, lane, v, x, y, z);
+            const uint32_t mat = load_mat<KIND>(mb, x, y, z);
+            qb[q0 + __popc(starts & lanemask_lt())] = dir_bits | (uint64_t)z << 36 | (uint64_t)y << 31 |
+                                                       (uint64_t)x << 26 | (uint64_t)(w - 1) << 21 |
+                                                       (uint64_t)(h - 1) << 16 | (uint64_t)mat;
           }
-          if (p.chunk_counts) {
-            const uint32_t tot = __reduce_add_sync(kFull, mine);
-            if (lane == 0) atomicAdd(&sm.chunk_quads, tot);
-          }
-        } else {
-          // isolated faces of 4 word groups; per group a warp-balanced
-          // expansion: lane j of round k emits the (k*32+j)-th set bit of the
-          // group, found by a shuffle binary search over the lanes' prefixes
-          // and __fns inside the owning word
-          for (int g = (task - 6) * 4; g < (task - 6) * 4 + 4; g++) {
-            if (sm.iso_count[g] == 0) continue;
-            const int dir = g >> 5, v = g & 31;
-            const uint32_t wv = sm.iso[dir][word_off(dir, lane, v)];
-            const uint32_t cw = __popc(wv);
-            uint32_t incl = cw;
-            for (int o = 1; o < 32; o <<= 1) {
-              const uint32_t y = __shfl_up_sync(kFull, incl, o);
-              if (lane >= o) incl += y;
-            }
-            const uint32_t ex = incl - cw;
-            const uint32_t G = __shfl_sync(kFull, incl, 31);
-            const unsigned long long base = sm.iso_base + sm.iso_off[g];
-            const uint64_t dir_bits = (uint64_t)((p.chunk_id_base + (uint32_t)c) & 0xFFFFFu) << 44 |
-                                      (uint64_t)dir << 41;
-            for (uint32_t k = 0; k < G; k += 32) {
-              const uint32_t j = k + (uint32_t)lane;
-              int l = 0;
-#pragma unroll
-              for (int step = 16; step >= 1; step >>= 1) {
-                const uint32_t oc = __shfl_sync(kFull, ex, l + step);
-                if (oc <= j) l += step;
-              }
-              const uint32_t wl = __shfl_sync(kFull, wv, l);
-              const uint32_t ol = __shfl_sync(kFull, ex, l);
-              if (j < G) {
-                const int u = (int)__fns(wl, 0, (int)(j - ol) + 1);
-                int x, y, z;
-                face_xyz(dir, l, u, v, x, y, z);
-                const uint32_t mat = load_mat<KIND>(mb, x, y, z);
-                const uint64_t q = dir_bits | (uint64_t)z << 36 | (uint64_t)y << 31 | (uint64_t)x << 26 | mat;
-                const unsigned long long idx = base + j;
-                if (idx < p.cap) p.quads[idx] = q;
-              }
-            }
-          }
+          __syncwarp();
+          if (lane == 0) sm.qcnt[warp] = q0 + cnt;
+          mine += cnt;
+          __syncwarp();
         }
       }
+      if (p.chunk_counts && lane == 0 && mine) atomicAdd(&sm.chunk_quads, mine);
     }
     __syncthreads();
     if (tid == 0) {
@@ -615,10 +622,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     buf ^= 1;
   }
-  if (warp < kGreedyWarps) {
-    uint32_t qc = sm.qcount[warp];
-    flush_quads(sm.qbuf[warp], qc, p, lane);
-  }
+  flush_warp(sm, warp, p, lane);
 }
 
 // --------------------------------------------------------------- host side
