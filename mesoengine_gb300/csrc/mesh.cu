@@ -505,44 +505,67 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       __syncthreads();
       const uint64_t chunk_bits = (uint64_t)((p.chunk_id_base + (uint32_t)c) & 0xFFFFFu) << 44;
-      // ---- pass 4a: isolated quads of this warp's 12 groups; per group a
-      // warp-balanced expansion: lane j of round k emits the (32k+j)-th set
-      // bit of the group, found by a shuffle binary search over the lanes'
-      // prefixes and __fns inside the owning word
+      // ---- pass 4a: isolated quads of this warp's 12 groups, 4 groups at a
+      // time so their shuffle chains interleave.  Per group a warp-balanced
+      // expansion: lane j of round k emits the (32k+j)-th set bit of the
+      // group, found by a shuffle binary search over the lanes' prefixes and
+      // __fns inside the owning word.
 #pragma unroll
-      for (int k = 0; k < 12; k++) {
-        const int g = warp + k * kWarps;
-        if (sm.iso_count[g] == 0) continue;
-        const int dir = g >> 5, v = g & 31;
-        const uint32_t wv = isow[k];
-        const uint32_t cw = __popc(wv);
-        uint32_t incl = cw;
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t y = __shfl_up_sync(kFull, incl, o);
-          if (lane >= o) incl += y;
+      for (int b = 0; b < 3; b++) {
+        uint32_t G[4], ex[4], wv[4];
+        bool any = false;
+#pragma unroll
+        for (int q = 0; q < 4; q++) any |= sm.iso_count[warp + (4 * b + q) * kWarps] != 0;
+        if (!any) continue;
+        uint32_t incl[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          wv[q] = isow[4 * b + q];
+          incl[q] = __popc(wv[q]);
         }
-        const uint32_t ex = incl - cw;
-        const uint32_t G = __shfl_sync(kFull, incl, 31);
-        const unsigned long long base = sm.iso_base + sm.iso_off[g];
-        const uint64_t dir_bits = chunk_bits | (uint64_t)dir << 41;
-        for (uint32_t k2 = 0; k2 < G; k2 += 32) {
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            const uint32_t y = __shfl_up_sync(kFull, incl[q], o);
+            if (lane >= o) incl[q] += y;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          ex[q] = incl[q] - __popc(wv[q]);
+          G[q] = __shfl_sync(kFull, incl[q], 31);
+        }
+        uint32_t maxG = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) maxG = G[q] > maxG ? G[q] : maxG;
+        for (uint32_t k2 = 0; k2 < maxG; k2 += 32) {
           const uint32_t j = k2 + (uint32_t)lane;
-          int l = 0;
+          int l[4] = {0, 0, 0, 0};
 #pragma unroll
           for (int step = 16; step >= 1; step >>= 1) {
-            const uint32_t oc = __shfl_sync(kFull, ex, l + step);
-            if (oc <= j) l += step;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              const uint32_t oc = __shfl_sync(kFull, ex[q], l[q] + step);
+              if (oc <= j) l[q] += step;
+            }
           }
-          const uint32_t wl = __shfl_sync(kFull, wv, l);
-          const uint32_t ol = __shfl_sync(kFull, ex, l);
-          if (j < G) {
-            const int u = (int)__fns(wl, 0, (int)(j - ol) + 1);
-            int x, y, z;
-            face_xyz(dir, l, u, v, x, y, z);
-            const uint32_t mat = load_mat<KIND>(mb, x, y, z);
-            const uint64_t q = dir_bits | (uint64_t)z << 36 | (uint64_t)y << 31 | (uint64_t)x << 26 | mat;
-            const unsigned long long idx = base + j;
-            if (idx < p.cap) p.quads[idx] = q;
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            const uint32_t wl = __shfl_sync(kFull, wv[q], l[q]);
+            const uint32_t ol = __shfl_sync(kFull, ex[q], l[q]);
+            if (j < G[q]) {
+              const int g = warp + (4 * b + q) * kWarps;
+              const int dir = g >> 5, v = g & 31;
+              const int u = (int)__fns(wl, 0, (int)(j - ol) + 1);
+              int x, y, z;
+              face_xyz(dir, l[q], u, v, x, y, z);
+              const uint32_t mat = load_mat<KIND>(mb, x, y, z);
+              const unsigned long long idx = sm.iso_base + sm.iso_off[g] + j;
+              if (idx < p.cap)
+                p.quads[idx] = chunk_bits | (uint64_t)dir << 41 | (uint64_t)z << 36 | (uint64_t)y << 31 |
+                               (uint64_t)x << 26 | mat;
+            }
           }
         }
       }
