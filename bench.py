@@ -38,6 +38,17 @@ L2_FLUSH_BYTES = 512 << 20
 MESH_CHUNKS = 4096
 
 
+def ncu_traffic(kernel):
+    """DRAM bytes (read + write) of one launch of `kernel` from the committed
+    ncu capture summary, or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_dram_bytes.json")) as f:
+            d = json.load(f)[kernel]
+        return int(d["dram_bytes_read"]) + int(d["dram_bytes_write"])
+    except Exception:
+        return None
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -426,7 +437,7 @@ def run_ours(args, world, rank, local, dist):
         "gpu_launches": int(r["launches"]),
         "roofline": {
             "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-            "frac": round(achieved / hbm, 4), "traffic": None, "peak_source": which,
+            "frac": round(achieved / hbm, 4), "traffic": ncu_traffic("raymarch_kernel"), "peak_source": which,
             "kernel": "raymarch_kernel",
             "algorithmic_bytes_per_launch": int(r["algo_bytes"]),
             "counts": r["counts"],
@@ -442,7 +453,7 @@ def run_ours(args, world, rank, local, dist):
             "batched_over_per_launch": round(m["ms_plain"] / m["ms"], 2),
             "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
                          "frac": round(ach / hbm, 4), "algorithmic_bytes_per_launch": m["algo_bytes"],
-                         "kernel": "mesh_kernel<CHUNKS_U16>"},
+                         "traffic": ncu_traffic("mesh_kernel<CHUNKS_U16>"), "kernel": "mesh_kernel<CHUNKS_U16>"},
         }
     if rank == 0 and not args.skip_serve:
         line["served"] = bench_serve_render(ctx, meso, args.serve_seconds)
