@@ -346,6 +346,47 @@ meso_status meso_server_drain(meso_server* srv, double timeout_s);
 double meso_server_now(const meso_server* srv);
 meso_status meso_server_destroy(meso_server* srv);
 
+/* ------------------------------------------------------------- downstream */
+
+/* Brick-map file: 32-byte header {char magic[8] = "MESOBRK1", uint32 version = 1,
+ * int32 nx, ny, nz, uint32 reserved, uint64 n_bricks}, then the pointer grid
+ * (uint32, live bricks renumbered 0..n-1 in pointer-grid order, the order a
+ * fresh build uses), then n occupancy masks (8 x uint64) and n material
+ * bricks (512 x uint16); little endian.  Lets resident scenes be saved and
+ * reloaded for reproducible serving runs (the reference regenerates chunks
+ * procedurally and has no scene file). */
+meso_status meso_scene_save(meso_ctx* ctx, const meso_scene* scene, const char* path);
+meso_status meso_scene_load(meso_ctx* ctx, const char* path, uint64_t spare_bricks, meso_scene** out);
+
+/* Vertex of an expanded quad: world position in voxel units and
+ * attr = material | dir << 16 | corner << 19. */
+typedef struct meso_vertex {
+  float x, y, z;
+  uint32_t attr;
+} meso_vertex;
+
+/* Expands n packed quads into 4 vertices each, counter-clockwise seen from
+ * outside the face; a quad of chunk index c sits at chunk_origin[c]*32 (int32
+ * triples, device).  The step after meshing for a raster consumer; replaces
+ * the reference's per-block FGPUBlock instance stream
+ * (Runtimes/Voxel/Block/Block.h:21-65) and the corner placement of its
+ * imposter vertex shader (Samples/SimpleVoxel.cpp:171-189). */
+meso_status meso_quads_to_vertices(meso_ctx* ctx, const uint64_t* d_quads, uint64_t n_quads,
+                                   const int32_t* d_chunk_origins, uint32_t n_chunks, meso_vertex* d_out,
+                                   void* stream);
+
+/* The reference's occupancy erosion pyramid on 32^3 chunks
+ * (FChunk::CalculateOccupancyErodeMipmaps, Runtimes/Voxel/Chunk/Chunk.h:73-94,
+ * with FOccupancyHelper::ErodeSingleVoxel,
+ * Runtimes/Voxel/Occupancy/BinaryOccupancyVolume.h:76-99): mip 0 is the
+ * occupancy; a voxel is set in mip d >= 1 iff it is set in mip 0, lies at
+ * least one voxel inside the chunk border, and all 26 neighbours are set in
+ * mip d-1.  d_out receives n * depth * 1024 uint32 words: chunk, mip, word
+ * (z, y) with bit x.  depth in 1..8.  The reference culls a block when mip 1
+ * has it set (Runtimes/Voxel/Chunk/ChunkPool.h:387). */
+meso_status meso_erode_mips(meso_ctx* ctx, const meso_mesh_source* src, const int32_t* d_chunk_coords,
+                            uint32_t n_chunks, uint32_t depth, uint32_t* d_out, void* stream);
+
 /* ------------------------------------------------------------------ graphs */
 
 /* CUDA-graph capture of a sequence of stream-ordered meso calls (meshing,

@@ -118,6 +118,8 @@ class ServerConfig(ctypes.Structure):
     ]
 
 
+VERTEX_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("attr", "<u4")])
+
 assert ctypes.sizeof(Camera) == 72
 assert HIT_DTYPE.itemsize == 24
 
@@ -181,6 +183,12 @@ _SIGNATURES = {
     "meso_server_drain": [ctypes.c_void_p, ctypes.c_double],
     "meso_server_destroy": [ctypes.c_void_p],
     "meso_autotune": [ctypes.c_void_p, ctypes.c_char_p],
+    "meso_scene_save": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p],
+    "meso_scene_load": [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)],
+    "meso_quads_to_vertices": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint32,
+                               ctypes.c_void_p, ctypes.c_void_p],
+    "meso_erode_mips": [ctypes.c_void_p, ctypes.POINTER(MeshSource), ctypes.c_void_p, ctypes.c_uint32,
+                        ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p],
     "meso_capture_begin": [ctypes.c_void_p, ctypes.c_void_p],
     "meso_capture_end": [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)],
     "meso_graph_launch": [ctypes.c_void_p, ctypes.c_void_p],
@@ -333,6 +341,9 @@ class Scene:
         for bz, by, bx in zip(*idx):
             out[bz, :, by, :, bx, :] = mat[p[bz, by, bx]].reshape(8, 8, 8)
         return out.reshape(nz, ny, nx)
+
+    def save(self, path: str) -> None:
+        _check(_lib.meso_scene_save(self.ctx.handle, self.handle, path.encode()))
 
     def edit(self, spheres, stream=None) -> np.ndarray:
         arr = (SphereEdit * max(1, len(spheres)))(*spheres)
@@ -548,6 +559,40 @@ class Context:
             rc = _lib.meso_capture_end(self.handle, stream, ctypes.byref(g))
         _check(rc)
         return Graph(g.value)
+
+    def scene_load(self, path: str, spare_bricks: int = 0) -> Scene:
+        h = ctypes.c_void_p()
+        _check(_lib.meso_scene_load(self.handle, path.encode(), spare_bricks, ctypes.byref(h)))
+        return Scene(self, h.value)
+
+    def quads_to_vertices(self, quads: np.ndarray, chunk_origins: np.ndarray) -> np.ndarray:
+        """Returns VERTEX_DTYPE records, 4 per quad."""
+        q = np.ascontiguousarray(quads, dtype=np.uint64)
+        org = np.ascontiguousarray(chunk_origins, dtype=np.int32).reshape(-1, 3)
+        dq, do = self.to_device(q if q.size else np.zeros(1, np.uint64)), self.to_device(org)
+        out = self.alloc(max(1, q.size) * 64)
+        _check(_lib.meso_quads_to_vertices(self.handle, dq.ptr, q.size, do.ptr, org.shape[0], out.ptr, None))
+        self.sync()
+        return out.download(VERTEX_DTYPE, 4 * q.size)
+
+    def erode_mips(self, kind, data=None, coords=None, n=None, dims=(0, 0, 0), scene=None, depth=4) -> np.ndarray:
+        """Erosion pyramid: uint32 words [n][depth][z][y] (bit x)."""
+        src = MeshSource()
+        src.kind = kind
+        src.d_data = data.ptr if isinstance(data, DeviceBuffer) else None
+        src.nx, src.ny, src.nz = dims
+        src.scene = scene.handle if scene is not None else None
+        cb = None
+        if coords is not None:
+            c = np.ascontiguousarray(coords, dtype=np.int32)
+            cb = self.to_device(c)
+            n = c.shape[0]
+            if kind in (SRC_CHUNKS_U16, SRC_CHUNKS_U8) and isinstance(data, DeviceBuffer):
+                src.nx = data.nbytes // (65536 if kind == SRC_CHUNKS_U16 else 32768)
+        out = self.alloc(n * depth * 4096)
+        _check(_lib.meso_erode_mips(self.handle, ctypes.byref(src), cb.ptr if cb else None, n, depth, out.ptr, None))
+        self.sync()
+        return out.download(np.uint32, n * depth * 1024).reshape(n, depth, 32, 32)
 
     def autotune(self, path: str | None = None) -> None:
         _check(_lib.meso_autotune(self.handle, path.encode() if path else None))

@@ -151,6 +151,7 @@ def lib() -> ctypes.CDLL:
         "mo_edit_spheres": (ctypes.c_int, [P(BrickMap), P(Sphere), u32]),
         "mo_dirty_chunks": (u32, [P(BrickMap), P(Sphere), u32, vp, u32]),
         "mo_hardware_threads": (ctypes.c_int, []),
+        "mo_erode_mips": (None, [vp, ctypes.c_int, ctypes.c_int, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -405,3 +406,47 @@ def raymarch_rows(bm: HostBrickMap, cam: Camera, row0: int, n_rows: int, light=N
 
 def hardware_threads() -> int:
     return int(lib().mo_hardware_threads())
+
+
+# ---------------------------------------------------------------- downstream
+
+def erode_mips(occ: np.ndarray, depth: int) -> np.ndarray:
+    """Erosion pyramid of one cubic chunk (occupancy [z][y][x]); returns
+    [depth][z][y][x] uint8 (the reference's CalculateOccupancyErodeMipmaps)."""
+    o = np.ascontiguousarray(occ != 0, dtype=np.uint8)
+    R = o.shape[0]
+    out = np.zeros((depth, R, R, R), dtype=np.uint8)
+    lib().mo_erode_mips(_ptr(o), R, depth, _ptr(out))
+    return out
+
+
+def quads_to_vertices(quads: np.ndarray, chunk_origins: np.ndarray) -> np.ndarray:
+    """Four corners per packed quad, counter-clockwise seen from outside:
+    returns float32 positions [n, 4, 3] and uint32 attributes [n, 4]
+    (material | dir << 16 | corner << 19), positions in world voxel units."""
+    u = unpack_quads(quads)
+    n = len(quads)
+    org = np.asarray(chunk_origins, dtype=np.int64).reshape(-1, 3)[u["chunk"]] * 32
+    d = u["dir"]
+    a = d // 2
+    plus = (d % 2) == 0
+    loc = np.stack([u["x"], u["y"], u["z"]], 1)
+    ua = np.where(a == 0, 1, 0)
+    va = np.where(a == 2, 1, 2)
+    pa = loc[np.arange(n), a] + plus
+    u0 = loc[np.arange(n), ua]
+    v0 = loc[np.arange(n), va]
+    natural = np.where(a == 1, ~plus, plus)
+    pos = np.zeros((n, 4, 3), dtype=np.int64)
+    attr = np.zeros((n, 4), dtype=np.uint32)
+    for k in range(4):
+        c = np.where(natural, k, (4 - k) % 4)
+        cu = np.where((c == 1) | (c == 2), u0 + u["w"], u0)
+        cv = np.where(c >= 2, v0 + u["h"], v0)
+        p = np.zeros((n, 3), dtype=np.int64)
+        p[np.arange(n), a] = pa
+        p[np.arange(n), ua] = cu
+        p[np.arange(n), va] = cv
+        pos[:, k] = p + org
+        attr[:, k] = (u["material"] | (d << 16) | (k << 19)).astype(np.uint32)
+    return pos.astype(np.float32), attr

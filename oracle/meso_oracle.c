@@ -992,3 +992,35 @@ uint32_t mo_dirty_chunks(const mo_brickmap* bm, const mo_sphere* s, uint32_t n, 
   if (c <= cap) qsort(out, c, sizeof(uint32_t), mo_cmp_u32);
   return c;
 }
+
+/* ======================================================================== */
+/* erosion pyramid (the reference's per-block loop, restated)               */
+/* ======================================================================== */
+
+void mo_erode_mips(const uint8_t* occ, int R, int depth, uint8_t* out) {
+  const size_t n = (size_t)R * R * R;
+  for (size_t i = 0; i < n; i++) out[i] = occ[i] != 0;
+  for (int d = 1; d < depth; d++) {
+    const uint8_t* last = out + (size_t)(d - 1) * n;
+    uint8_t* cur = out + (size_t)d * n;
+    memset(cur, 0, n);
+    for (int z = 0; z < R; z++)
+      for (int y = 0; y < R; y++)
+        for (int x = 0; x < R; x++) {
+          if (!occ[(size_t)x + (size_t)R * (y + (size_t)R * z)]) continue; /* only the chunk's blocks */
+          /* bIsOutOfBoundThickness(Location, R, 1) -> not eroded-solid */
+          if (x < 1 || x >= R - 1 || y < 1 || y >= R - 1 || z < 1 || z >= R - 1) continue;
+          int solid = 1;
+          for (int dz = -1; dz <= 1 && solid; dz++)
+            for (int dy = -1; dy <= 1 && solid; dy++)
+              for (int dx = -1; dx <= 1; dx++) {
+                if (!dx && !dy && !dz) continue;
+                if (!last[(size_t)(x + dx) + (size_t)R * ((y + dy) + (size_t)R * (z + dz))]) {
+                  solid = 0;
+                  break;
+                }
+              }
+          cur[(size_t)x + (size_t)R * (y + (size_t)R * z)] = (uint8_t)solid;
+        }
+  }
+}

@@ -192,6 +192,16 @@ int mo_edit_spheres(mo_brickmap* bm, const mo_sphere* s, uint32_t n);
 uint32_t mo_dirty_chunks(const mo_brickmap* bm, const mo_sphere* s, uint32_t n, uint32_t* out,
                          uint32_t cap);
 
+/* ---- erosion pyramid ----------------------------------------------------- */
+/* Restates FChunk::CalculateOccupancyErodeMipmaps (Runtimes/Voxel/Chunk/Chunk.h:73-94)
+ * with FOccupancyHelper::ErodeSingleVoxel<true>
+ * (Runtimes/Voxel/Occupancy/BinaryOccupancyVolume.h:76-99) on one R^3 chunk
+ * (R = 32 here): mip 0 = occupancy; for d >= 1, every voxel of mip 0 is
+ * tested: out of the border thickness 1 (VoxelMathHelper.h:106-112) -> 0,
+ * else the AND of its 26 Moore neighbours in mip d-1.  occ: R^3 bytes
+ * (nonzero = solid, x fastest); out: depth * R^3 bytes. */
+void mo_erode_mips(const uint8_t* occ, int R, int depth, uint8_t* out);
+
 int mo_hardware_threads(void);
 
 #ifdef __cplusplus

@@ -255,3 +255,39 @@ def test_generators_are_deterministic():
     assert oracle.lib().mo_pcg3d(1, 2, 3) == oracle.lib().mo_pcg3d(1, 2, 3)
     v = oracle.lib().mo_vnoise3(5, 6, 7, 64, 1)
     assert 0.0 <= v < 1.0
+
+
+# ------------------------------------------------------ downstream restatements
+
+def test_erosion_pyramid_of_a_solid_chunk():
+    occ = np.ones((32, 32, 32), np.uint8)
+    m = oracle.erode_mips(occ, 5)
+    for d in range(5):
+        z, y, x = np.indices((32, 32, 32))
+        expect = ((x >= d) & (x <= 31 - d) & (y >= d) & (y <= 31 - d) & (z >= d) & (z <= 31 - d)) if d else occ > 0
+        assert np.array_equal(m[d] > 0, expect), d
+
+
+def test_erosion_needs_all_26_neighbours():
+    occ = np.zeros((32, 32, 32), np.uint8)
+    occ[9:12, 9:12, 9:12] = 1          # a 3^3 block: only its centre is enclosed
+    m = oracle.erode_mips(occ, 3)
+    assert m[1].sum() == 1 and m[1][10, 10, 10] == 1
+    assert m[2].sum() == 0
+    occ[9, 9, 9] = 0                    # remove one corner: the centre is no longer enclosed
+    assert oracle.erode_mips(occ, 2)[1].sum() == 0
+
+
+def test_quad_vertices_known_corners():
+    q = np.array([oracle.lib().mo_pack_quad(0, 4, 2, 3, 5, 4, 2, 9),   # +Z at z=5, x 2..6, y 3..5
+                  oracle.lib().mo_pack_quad(1, 1, 7, 0, 0, 1, 1, 3)],  # -X at x=7 of chunk 1
+                 dtype=np.uint64)
+    pos, attr = oracle.quads_to_vertices(q, [(0, 0, 0), (1, 0, 2)])
+    assert pos[0].tolist() == [[2, 3, 6], [6, 3, 6], [6, 5, 6], [2, 5, 6]]
+    # -X: plane x = 7 (+32 origin), reversed corner order
+    assert pos[1].tolist() == [[39, 0, 64], [39, 0, 65], [39, 1, 65], [39, 1, 64]]
+    assert (attr[0] & 0xFFFF).tolist() == [9] * 4 and ((attr[1] >> 16) & 7).tolist() == [1] * 4
+    # counter-clockwise seen from outside: (p1 - p0) x (p2 - p0) is along the normal
+    for i, normal in ((0, (0, 0, 1)), (1, (-1, 0, 0))):
+        n = np.cross(pos[i, 1] - pos[i, 0], pos[i, 2] - pos[i, 0])
+        assert np.array_equal(np.sign(n), np.array(normal))
