@@ -127,6 +127,26 @@ __device__ __forceinline__ uint32_t load_mat(const uint8_t* buf, int x, int y, i
   }
 }
 
+// True iff the 8 rows y0..y0+7 (y0 % 8 == 0) of slab z are all empty: one
+// 16-byte (8-byte for uint8) shared load per lane covers the 256 voxels.
+template <int KIND>
+__device__ __forceinline__ bool rows8_empty(const uint8_t* buf, int y0, int z, int lane) {
+  using T = KindTraits<KIND>;
+  bool nz;
+  if constexpr (T::kBrick) {
+    const int b = (lane >> 3) + 4 * (y0 >> 3) + 16 * (z >> 3);
+    const uint4 w = *reinterpret_cast<const uint4*>(buf + b * kBrickSlot + 128 * (z & 7) + 16 * (lane & 7));
+    nz = (w.x | w.y | w.z | w.w) != 0;
+  } else if constexpr (T::kElem == 2) {
+    const uint4 w = *reinterpret_cast<const uint4*>(buf + (z * 32 + y0) * 64 + 16 * lane);
+    nz = (w.x | w.y | w.z | w.w) != 0;
+  } else {
+    const uint2 w = *reinterpret_cast<const uint2*>(buf + (z * 32 + y0) * 32 + 8 * lane);
+    nz = (w.x | w.y) != 0;
+  }
+  return !__any_sync(kFull, nz);
+}
+
 // Occupancy (material != 0) of a global voxel for halo reads; 0 outside.
 template <int KIND>
 __device__ __forceinline__ uint32_t global_solid(const MeshParams& p, int gx, int gy, int gz) {
@@ -375,6 +395,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int z = warp; z < 32; z += kWarps) {
         uint32_t r_occ = 0, r_ex = 0, r_ey = 0, r_ez = 0, prev_m = 0;
         for (int y0 = 0; y0 < 32; y0 += 8) {
+          if (rows8_empty<KIND>(mb, y0, z, lane)) {
+            prev_m = 0;  // row y0+7 is empty; nothing to capture
+            continue;
+          }
           // 8 rows at a time: all loads first, then the votes
           const int dl = lane - y0;  // row captured by this lane, if in 0..7
           uint32_t m[8], occw[8];
@@ -577,6 +601,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       // a quad's height is one ballot over the rows below, and the quads of
       // one row never interact because their columns are disjoint.
       uint64_t* qb = sm.qbuf[warp];
+      uint32_t qc = sm.qcnt[warp];  // warp-uniform count of staged quads
       uint32_t mine = 0;
       for (;;) {
         int task = 0;
@@ -603,8 +628,12 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t link = word & e & (word << 1);
           const uint32_t starts = word & ~link;
           const uint32_t cnt = __popc(starts);
-          if (sm.qcnt[warp] + cnt > (uint32_t)kQBuf) flush_warp(sm, warp, p, lane);
-          const uint32_t q0 = sm.qcnt[warp];
+          if (qc + cnt > (uint32_t)kQBuf) {
+            if (lane == 0) sm.qcnt[warp] = qc;
+            flush_warp(sm, warp, p, lane);
+            qc = 0;
+          }
+          const uint32_t q0 = qc;
           // every start lane grows its quad; row r's words come from lane r
           const bool is_start = (starts >> lane) & 1u;
           const int w = __ffs(~__funnelshift_rc(link, 0u, (uint32_t)lane + 1u));
@@ -629,12 +658,12 @@ __global__ void __launch_bounds__(kThreads, 1)
                                                        (uint64_t)x << 26 | (uint64_t)(w - 1) << 21 |
                                                        (uint64_t)(h - 1) << 16 | (uint64_t)mat;
           }
-          __syncwarp();
-          if (lane == 0) sm.qcnt[warp] = q0 + cnt;
+          qc = q0 + cnt;
           mine += cnt;
-          __syncwarp();
         }
       }
+      if (lane == 0) sm.qcnt[warp] = qc;
+      __syncwarp();
       if (p.chunk_counts && lane == 0 && mine) atomicAdd(&sm.chunk_quads, mine);
     }
     __syncthreads();
