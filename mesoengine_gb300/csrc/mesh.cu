@@ -54,6 +54,7 @@ struct __align__(128) MeshSmem {
   uint32_t halo[6][32];                   // -X,+X: bits y by z; -Y,+Y: bits x by z; -Z,+Z: bits x by y
   uint64_t qbuf[kWarps][kQBuf];           // staged greedy quads per warp
   uint32_t rest_rows[192];                // per slice 32*dir + s: rows holding non-isolated faces
+  uint16_t rest_list[192];                // slices with non-isolated faces, in discovery order
   uint64_t bar[2];
   int32_t chunk[2];
   int32_t valid[2];
@@ -63,6 +64,7 @@ struct __align__(128) MeshSmem {
   uint32_t iso_off[192];             // their exclusive prefix within the chunk
   unsigned long long iso_base;       // global offset of the chunk's isolated quads
   uint32_t task_next;                // dynamic task counter of pass 4
+  uint32_t rest_n;                   // entries of rest_list
   uint32_t qcnt[kWarps];             // staged quads in qbuf[warp]
 };
 
@@ -359,7 +361,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (tid < 192) sm.iso_count[tid] = 0;
   if (tid < 192) sm.rest_rows[tid] = 0;
   if (tid < kWarps) sm.qcnt[tid] = 0;
-  if (tid == 0) sm.task_next = 0;
+  if (tid == 0) {
+    sm.task_next = 0;
+    sm.rest_n = 0;
+  }
   __syncthreads();
   if (warp == 0) issue_chunk<KIND>(sm, p, &tmap, 0, lane, cur, end);
   __syncthreads();
@@ -442,9 +447,12 @@ __global__ void __launch_bounds__(kThreads, 1)
           sm.f[2][o] = r_occ & ~up;  // +Y, [z][y]
           sm.f[3][o] = r_occ & ~dn;  // -Y
         }
-        const uint32_t occT = transpose32(r_occ, lane);
-        const uint32_t eyT = transpose32(r_ey, lane);
-        const uint32_t ezT = transpose32(r_ez, lane);
+        uint32_t occT = 0, eyT = 0, ezT = 0;
+        if (__any_sync(kFull, r_occ != 0)) {  // an empty slab has no X faces
+          occT = transpose32(r_occ, lane);
+          eyT = transpose32(r_ey, lane);
+          ezT = transpose32(r_ez, lane);
+        }
         uint32_t up = __shfl_down_sync(kFull, occT, 1), dn = __shfl_up_sync(kFull, occT, 1);
         if (lane == 31) up = sm.halo[1][z];
         if (lane == 0) dn = sm.halo[0][z];
@@ -501,7 +509,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int o = word_off(d, sl, v);
         const uint32_t rest = sm.f[d][o] & ~isow[k];
         sm.f[d][o] = rest;
-        if (rest) atomicOr(&sm.rest_rows[d * 32 + sl], 1u << v);
+        if (rest) {
+          // the first row of a slice to hold non-isolated faces lists the slice
+          if (atomicOr(&sm.rest_rows[d * 32 + sl], 1u << v) == 0u)
+            sm.rest_list[atomicAdd(&sm.rest_n, 1u)] = (uint16_t)(d * 32 + sl);
+        }
       }
       if (warp == kWarps - 1) {
         // exclusive prefix over the 192 word groups (6 per lane) and one
@@ -603,13 +615,14 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint64_t* qb = sm.qbuf[warp];
       uint32_t qc = sm.qcnt[warp];  // warp-uniform count of staged quads
       uint32_t mine = 0;
+      const uint32_t n_tasks = sm.rest_n;
       for (;;) {
-        int task = 0;
-        if (lane == 0) task = (int)atomicAdd(&sm.task_next, 1u);
-        task = __shfl_sync(kFull, task, 0);
-        if (task >= 192) break;
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(&sm.task_next, 1u);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= n_tasks) break;
+        const int task = sm.rest_list[t];
         uint32_t rows = sm.rest_rows[task];
-        if (!rows) continue;
         if (lane == 0) sm.rest_rows[task] = 0;
         const int dir = task >> 5, sl = task & 31;
         const int orow = word_off(dir, sl, lane);
@@ -671,6 +684,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (p.chunk_counts) p.chunk_counts[c] = valid ? sm.chunk_quads : 0u;
       sm.chunk_quads = 0;
       sm.task_next = 0;
+      sm.rest_n = 0;
     }
     buf ^= 1;
   }
