@@ -58,7 +58,7 @@ typedef struct meso_config {
   uint32_t mesh_ctas_per_sm;      /* persistent mesher CTAs per SM (0 = tuned/default 1) */
   uint32_t mesh_chunks_per_ticket;/* chunks taken per queue ticket (0 = tuned/default 1) */
   uint32_t ray_tile_w, ray_tile_h;/* threads of one ray CTA tile (0 = tuned/default 8x4 per warp) */
-  uint32_t ray_warps_per_cta;     /* 0 = tuned/default */
+  uint32_t ray_warps_per_cta;     /* 1..4, 0 = tuned/default */
   uint64_t hbm_budget_bytes;      /* admission budget for resident scenes + requests (0 = 90% of free) */
   const char* tuning_path;        /* optional tuning JSON written by meso_autotune */
 } meso_config;

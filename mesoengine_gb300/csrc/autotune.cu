@@ -70,7 +70,7 @@ extern "C" meso_status meso_autotune(meso_ctx* ctx, const char* path) {
   const meso_scene* sc = scene;
   float best_ray = 1e30f;
   Tuning best = saved;
-  const uint32_t tws[4] = {4, 8, 16, 32}, wpcs[3] = {2, 4, 8};
+  const uint32_t tws[4] = {4, 8, 16, 32}, wpcs[3] = {1, 2, 4};  // the kernel allows at most 128 threads per CTA
   for (uint32_t tw : tws) {
     for (uint32_t wpc : wpcs) {
       if (rc != MESO_OK) break;
