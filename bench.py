@@ -326,18 +326,29 @@ def bench_serve_render(ctx, meso, seconds, rate=2000.0):
     srv.close()
     res = summarize(comps)
     res["offered_mrays_s"] = round(sum(it[2].width * it[2].height for it in items) / seconds / 1e6, 1)
-    # plain form: one launch per request, waited for one at a time
-    k = min(300, len(items))
+    # capacity: the first K requests submitted at once (no arrival pacing)
+    k = min(2000, len(items))
+    srv = meso.Server(ctx, scenes, max_inflight_batches=4, max_batch_rays=16 << 20, hbm_budget_bytes=120 << 30)
+    t0 = time.perf_counter()
+    for it in items[:k]:
+        srv.submit(it[1], it[2], shadow=False)
+    srv.drain(600.0)
+    burst_s = time.perf_counter() - t0
+    burst = srv.poll(1 << 16)
+    srv.close()
+    px = sum(it[2].width * it[2].height for it in items[:k])
+    res["capacity_mrays_s"] = round(px / burst_s / 1e6, 1)
+    # plain form: the same K requests, one launch per request, each waited for
+    out = ctx.alloc(3840 * 2160 * 24)
     ctx.sync()
     t0 = time.perf_counter()
-    px = 0
     for it in items[:k]:
-        out = ctx.raymarch(scenes[it[1]], it[2], shadow=False, download=False)
+        ctx.raymarch(scenes[it[1]], it[2], shadow=False, out=out, download=False)
         ctx.sync()
-        px += it[2].width * it[2].height
-        out.free()
     res["plain_per_view_mrays_s"] = round(px / (time.perf_counter() - t0) / 1e6, 1)
-    res["served_over_plain"] = round(res["mrays_s"] / max(res["plain_per_view_mrays_s"], 1e-9), 2)
+    res["capacity_over_plain"] = round(res["capacity_mrays_s"] / max(res["plain_per_view_mrays_s"], 1e-9), 2)
+    res["capacity_requests"] = k
+    assert all(c.status == 0 for c in burst)
     res["workload"] = (f"4 resident scenes {dims}, Poisson {rate:.0f} req/s for {seconds:.0f} s (seed 7), "
                        "sizes {256^2, 512^2, 1920x1080, 3840x2160}, primary rays, HBM budget 120 GB")
     for s in scenes:
@@ -377,6 +388,51 @@ def bench_serve_edit(ctx, meso, seconds, rate=200.0):
     res["gvox_meshed_s_busy"] = round(chunks * 32768 / max(busy, 1e-9) / 1e9, 3)
     res["workload"] = (f"4096^3 terrain (512^3 pointer grid), Poisson {rate:.0f} req/s for {seconds:.0f} s (seed 9), "
                        "1-32 sphere edits + remesh of dirty chunks + 1920x1080 primary render")
+    # capacity (requests submitted at once) and the plain form (edit, one mesh
+    # launch per dirty chunk, one render launch, waited for) on fresh copies
+    k = min(200, len(items))
+    scene.destroy()
+    scene = ctx.scene_from_terrain(t, spare_bricks=4 << 20)
+    srv = meso.Server(ctx, [scene], max_inflight_batches=4, max_batch_rays=4 << 20, max_edit_quads=64 << 20)
+    t0 = time.perf_counter()
+    for it in items[:k]:
+        srv.submit(0, it[2], shadow=False, edits=it[1])
+    srv.drain(600.0)
+    cap_s = time.perf_counter() - t0
+    comps = srv.poll(1 << 16)
+    srv.close()
+    cap_chunks = sum(c.n_dirty_chunks for c in comps)
+    scene.destroy()
+    scene = ctx.scene_from_terrain(t, spare_bricks=4 << 20)
+    qbuf, cnt = ctx.alloc((64 << 20) * 8), ctx.alloc(8)
+    hits = ctx.alloc(1920 * 1080 * 24)
+    cx = n // 32
+    src = meso.MeshSource()
+    src.kind = meso.SRC_BRICKMAP
+    src.scene = scene.handle
+    mo = meso.MeshOutput(qbuf.ptr, 64 << 20, cnt.ptr, None)
+    import ctypes
+    L = meso._lib
+    plain_chunks = 0
+    ctx.sync()
+    t0 = time.perf_counter()
+    for it in items[:k]:
+        dirty = scene.edit(it[1])
+        if len(dirty):
+            coords = np.stack([dirty % cx, (dirty // cx) % cx, dirty // (cx * cx)], 1).astype(np.int32)
+            cb = ctx.to_device(coords)
+            meso._check(L.meso_mesh_chunks_per_launch(ctx.handle, ctypes.byref(src), cb.ptr, len(dirty),
+                                                      ctypes.byref(mo), None))
+            plain_chunks += len(dirty)
+        ctx.raymarch(scene, it[2], shadow=False, out=hits, download=False)
+        ctx.sync()
+    plain_s = time.perf_counter() - t0
+    res["capacity_requests"] = k
+    res["capacity_req_s"] = round(k / cap_s, 1)
+    res["capacity_gvox_meshed_s"] = round(cap_chunks * 32768 / cap_s / 1e9, 3)
+    res["plain_req_s"] = round(k / plain_s, 1)
+    res["plain_gvox_meshed_s"] = round(plain_chunks * 32768 / plain_s / 1e9, 3)
+    res["capacity_over_plain"] = round(res["capacity_req_s"] / max(res["plain_req_s"], 1e-9), 2)
     scene.destroy()
     return res
 
