@@ -8,21 +8,24 @@
 // (Runtimes/Voxel/Chunk/ChunkManager.h:183-210).  Here a persistent kernel
 // pulls chunks from a device ticket queue and emits greedy quads.
 //
-// Per chunk (one CTA, 8 warps):
+// Two CTAs of 8 warps share each SM, each meshing its own chunk, so one
+// CTA's barrier-separated phases overlap the other's work.  Per chunk:
 //  1. staging: the 32^3 materials arrive in shared memory through TMA (one
 //     bulk copy per chunk of a chunk array, one 3-D tensor box per chunk of a
-//     dense grid, one 1 KiB bulk copy per occupied brick of a brick map),
-//     double-buffered so the next chunk streams in while this one is meshed;
-//     the one-voxel occupancy halo is read with plain loads meanwhile;
+//     dense grid, one 1 KiB bulk copy per occupied brick of a brick map); the
+//     one-voxel occupancy halo is read with plain loads while it lands;
 //  2. masks: lanes = x; every row (y,z) becomes bit-packed words with warp
-//     ballots: occupancy, material-equality with the -x, -y and -z neighbour,
-//     and (accumulated per lane over y) the transposed columns for the X
-//     faces; face masks are occ & ~shift(occ) per direction;
-//  3. greedy: warp = face direction, lane = slice; rows are scanned with
-//     ffs / run-length bit tricks (Lysenko's order: first unconsumed face,
-//     widen along u while the material matches, grow along v while the whole
-//     run matches); quads are staged per warp in shared memory and appended
-//     to global memory with one atomic per ~480 quads.
+//     ballots: occupancy and material-equality with the -x, -y and -z
+//     neighbour, plus warp-transposed copies (bits over y) for the X faces;
+//     face masks occ & ~shift(occ) are recomputed from these where needed;
+//  3. isolated faces (no same-material face neighbour in their plane) are
+//     peeled off in registers and emitted as 1x1 quads by a warp-balanced
+//     expansion, one output reservation per warp and chunk;
+//  4. greedy: warp = slice with non-isolated faces, lane = row; rows are
+//     scanned with run-length bit tricks (Lysenko's order: first unconsumed
+//     face, widen along u while the material matches, grow along v while the
+//     whole run matches); quads are staged per warp in shared memory and
+//     appended to global memory with one atomic per 128 quads.
 #include <cudaTypedefs.h>
 
 #include <cstdio>
@@ -35,38 +38,36 @@ namespace {
 
 using namespace ::meso::dev;
 
-constexpr int kThreads = 512;
+constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
+constexpr int kGroups = 192 / kWarps;  // word groups (direction, row) per warp: 4 rows x 6 directions
+static_assert(kWarps * 4 == 32, "the isolated-face pass gives each warp 4 rows");
 constexpr int kS = 33;               // padded row stride of 32x32 word arrays
 constexpr int kArr = 32 * kS;
-constexpr int kQBuf = 256;           // staged quads per warp
+constexpr int kQBuf = 128;           // staged quads per warp
 constexpr int kBrickSlot = 1040;     // bytes per staged brick (bank-spread padding)
 constexpr int kMatBuf = 64 * kBrickSlot;
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 
 struct __align__(128) MeshSmem {
-  uint8_t mat[2][kMatBuf];
-  uint32_t occ[kArr];
+  uint8_t mat[kMatBuf];
+  uint32_t occ[kArr];                     // occupancy, bits over x, [z][y]
+  uint32_t occt[kArr];                    // occupancy, bits over y, [z][x]
   uint32_t ex[kArr], ey[kArr], ez[kArr];  // equality with -x / -y / -z neighbour, bits over x, [z][y]
   uint32_t eyt[kArr], ezt[kArr];          // equality with -y / -z neighbour, bits over y, [z][x]
-  uint32_t f[6][kArr];                    // face masks; X: [z][x] bits y; Y,Z: [z][y] bits x
   uint32_t halo[6][32];                   // -X,+X: bits y by z; -Y,+Y: bits x by z; -Z,+Z: bits x by y
   uint64_t qbuf[kWarps][kQBuf];           // staged greedy quads per warp
-  uint32_t rest_rows[192];                // per slice 32*dir + s: rows holding non-isolated faces
-  uint16_t rest_list[192];                // slices with non-isolated faces, in discovery order
-  uint64_t bar[2];
-  int32_t chunk[2];
-  int32_t valid[2];
-  int32_t coord[2][3];
+  uint32_t rest_slices[6];                // per direction: bit s = slice s holds non-isolated faces
+  uint64_t bar;
+  int32_t chunk;
+  int32_t valid;
+  int32_t coord[3];
   uint32_t chunk_quads;
-  uint32_t iso_count[192];           // isolated quads per word group g = 32*dir + row
-  uint32_t iso_off[192];             // their exclusive prefix within the chunk
-  unsigned long long iso_base;       // global offset of the chunk's isolated quads
-  uint32_t task_next;                // dynamic task counter of pass 4
-  uint32_t rest_n;                   // entries of rest_list
-  uint32_t qcnt[kWarps];             // staged quads in qbuf[warp]
+  uint32_t task_next;                     // dynamic task counter of the greedy
+  uint32_t any_solid;
 };
+static_assert(sizeof(MeshSmem) + 128 <= 113 * 1024, "two mesher CTAs must fit in one SM");
 
 struct MeshParams {
   const uint8_t* data;
@@ -169,17 +170,21 @@ __device__ __forceinline__ uint32_t global_solid(const MeshParams& p, int gx, in
 }
 
 // Producer side: called by warp 0 (all lanes).  Takes the next chunk off the
-// queue and starts its copy into buffer `buf`.
+// queue and starts its copy into the staging buffer.  Lane 0 holds the queue
+// state: [cur, end) is the current ticket's range and `pending` the start of
+// the next ticket, requested one ticket ahead so the atomic's latency is
+// hidden behind a chunk's work.
 template <int KIND>
-__device__ __forceinline__ void issue_chunk(MeshSmem& sm, const MeshParams& p, const CUtensorMap* tmap, int buf,
-                                            int lane, uint32_t& cur, uint32_t& end) {
+__device__ __forceinline__ void issue_chunk(MeshSmem& sm, const MeshParams& p, const CUtensorMap* tmap, int lane,
+                                            uint32_t& cur, uint32_t& end, uint32_t& pending) {
   using T = KindTraits<KIND>;
   int c = -1;
   if (lane == 0) {
     if (p.use_queue) {
       if (cur >= end) {
-        cur = atomicAdd(p.ticket, p.per_ticket);
+        cur = pending;
         end = cur + p.per_ticket;
+        pending = atomicAdd(p.ticket, p.per_ticket);
       }
       if (cur < p.n_chunks) c = (int)cur++;
     } else {
@@ -190,16 +195,16 @@ __device__ __forceinline__ void issue_chunk(MeshSmem& sm, const MeshParams& p, c
     }
   }
   c = __shfl_sync(kFull, c, 0);
-  if (lane == 0) sm.chunk[buf] = c;
+  if (lane == 0) sm.chunk = c;
   if (c < 0) return;
-  uint64_t* bar = &sm.bar[buf];
-  uint8_t* dst = sm.mat[buf];
+  uint64_t* bar = &sm.bar;
+  uint8_t* dst = sm.mat;
   if constexpr (!T::kGrid && !T::kBrick) {
     if (lane == 0) {
       // with an index list, p.nx is the number of chunks in the array
       const uint32_t idx = p.coords ? (uint32_t)p.coords[c] : (uint32_t)c;
       const bool ok = !p.coords || idx < (uint32_t)p.nx;
-      sm.valid[buf] = ok ? 1 : 0;
+      sm.valid = ok ? 1 : 0;
       if (!ok) {
         atomicOr(p.err, ERR_BAD_INPUT);
         mbar_arrive_expect_tx(bar, 0);
@@ -233,10 +238,10 @@ __device__ __forceinline__ void issue_chunk(MeshSmem& sm, const MeshParams& p, c
     }
     const bool ok = cx >= 0 && cy >= 0 && cz >= 0 && cx < lim_x && cy < lim_y && cz < lim_z;
     if (lane == 0) {
-      sm.coord[buf][0] = cx;
-      sm.coord[buf][1] = cy;
-      sm.coord[buf][2] = cz;
-      sm.valid[buf] = ok ? 1 : 0;
+      sm.coord[0] = cx;
+      sm.coord[1] = cy;
+      sm.coord[2] = cz;
+      sm.valid = ok ? 1 : 0;
     }
     if (!ok) {
       if (lane == 0) {
@@ -281,8 +286,8 @@ __device__ __forceinline__ void issue_chunk(MeshSmem& sm, const MeshParams& p, c
 }
 
 template <int KIND>
-__device__ __forceinline__ void compute_halos(MeshSmem& sm, const MeshParams& p, int buf, int warp, int lane) {
-  const int X = sm.coord[buf][0] * 32, Y = sm.coord[buf][1] * 32, Z = sm.coord[buf][2] * 32;
+__device__ __forceinline__ void compute_halos(MeshSmem& sm, const MeshParams& p, int warp, int lane) {
+  const int X = sm.coord[0] * 32, Y = sm.coord[1] * 32, Z = sm.coord[2] * 32;
   for (int wi = warp; wi < 6 * 32; wi += kWarps) {
     const int f = wi >> 5, k = wi & 31;
     int gx, gy, gz;
@@ -323,10 +328,64 @@ __device__ __forceinline__ void face_xyz(int d, int s, int u, int v, int& x, int
   else { x = u; y = v; z = s; }
 }
 
+// In-plane equality arrays of direction d: E along u, V along v.
+__device__ __forceinline__ const uint32_t* e_arr(const MeshSmem& sm, int d) { return d < 2 ? sm.eyt : sm.ex; }
+__device__ __forceinline__ const uint32_t* v_arr(const MeshSmem& sm, int d) {
+  return d < 2 ? sm.ezt : (d < 4 ? sm.ez : sm.ey);
+}
+
+// Face word of direction d, row v, for the slice s = lane (all lanes call):
+// the occupancy word of the slice minus that of the next slice along the
+// face normal, taken from the neighbouring lane or the halo.
+__device__ __forceinline__ uint32_t face_row(const MeshSmem& sm, int d, int v, int lane) {
+  uint32_t c, hi, lo;
+  if (d < 2) {
+    c = sm.occt[v * kS + lane];
+    hi = sm.halo[1][v];
+    lo = sm.halo[0][v];
+  } else if (d < 4) {
+    c = sm.occ[v * kS + lane];
+    hi = sm.halo[3][v];
+    lo = sm.halo[2][v];
+  } else {
+    c = sm.occ[lane * kS + v];
+    hi = sm.halo[5][v];
+    lo = sm.halo[4][v];
+  }
+  uint32_t n;
+  if ((d & 1) == 0) {
+    n = __shfl_down_sync(kFull, c, 1);
+    if (lane == 31) n = hi;
+  } else {
+    n = __shfl_up_sync(kFull, c, 1);
+    if (lane == 0) n = lo;
+  }
+  return c & ~n;
+}
+
+// Face word of direction d, slice s, for the row v = r (lanes = rows).
+__device__ __forceinline__ uint32_t face_col(const MeshSmem& sm, int d, int s, int r) {
+  const bool pos = (d & 1) == 0;
+  const int sn = pos ? s + 1 : s - 1;
+  const bool edge = pos ? s == 31 : s == 0;
+  // halo[d ^ 1] is the layer beyond the chunk on the side the face points to
+  if (d < 2) return sm.occt[r * kS + s] & ~(edge ? sm.halo[d ^ 1][r] : sm.occt[r * kS + sn]);
+  if (d < 4) return sm.occ[r * kS + s] & ~(edge ? sm.halo[d ^ 1][r] : sm.occ[r * kS + sn]);
+  return sm.occ[s * kS + r] & ~(edge ? sm.halo[d ^ 1][r] : sm.occ[sn * kS + r]);
+}
+
+// Faces of a word with a same-material face neighbour in the plane: f the
+// faces of the row, fu / fd those of rows v-1 / v+1, e equality with the -u
+// neighbour, vv / vd equality of this row / of row v+1 with the row above.
+__device__ __forceinline__ uint32_t isolated(uint32_t f, uint32_t fu, uint32_t fd, uint32_t e, uint32_t vv,
+                                             uint32_t vd) {
+  const uint32_t left = f & e & (f << 1);
+  return f & ~(left | (left >> 1) | (f & vv & fu) | (f & vd & fd));
+}
+
 // Appends the warp's staged quads to the output (one atomic per flush).
-__device__ __forceinline__ void flush_warp(MeshSmem& sm, int warp, const MeshParams& p, int lane) {
+__device__ __forceinline__ void flush_warp(MeshSmem& sm, int warp, const MeshParams& p, int lane, uint32_t cnt) {
   __syncwarp();
-  const uint32_t cnt = sm.qcnt[warp];
   unsigned long long base = 0;
   if (lane == 0 && cnt) base = atomicAdd(p.count, (unsigned long long)cnt);
   base = __shfl_sync(kFull, base, 0);
@@ -335,12 +394,10 @@ __device__ __forceinline__ void flush_warp(MeshSmem& sm, int warp, const MeshPar
     if (idx < p.cap) p.quads[idx] = sm.qbuf[warp][i];
   }
   __syncwarp();
-  if (lane == 0) sm.qcnt[warp] = 0;
-  __syncwarp();
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, 2)
     mesh_kernel(const MeshParams p, const __grid_constant__ CUtensorMap tmap) {
   using T = KindTraits<KIND>;
   extern __shared__ uint8_t smem_raw[];
@@ -349,54 +406,47 @@ __global__ void __launch_bounds__(kThreads, 1)
   MeshSmem& sm = *reinterpret_cast<MeshSmem*>(smem_raw + pad);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  uint32_t cur = p.use_queue ? 0u : blockIdx.x, end = 0;
+  uint32_t cur = p.use_queue ? 0u : blockIdx.x, end = 0, pending = 0;
 
   if (tid == 0) {
-    mbar_init(&sm.bar[0], 1);
-    mbar_init(&sm.bar[1], 1);
+    mbar_init(&sm.bar, 1);
     sm.chunk_quads = 0;
+    sm.task_next = 0;
+    sm.any_solid = 0;
     fence_proxy_async_smem();
+    if (p.use_queue) pending = atomicAdd(p.ticket, p.per_ticket);
   }
   for (int i = tid; i < 6 * 32; i += kThreads) (&sm.halo[0][0])[i] = 0;
-  if (tid < 192) sm.iso_count[tid] = 0;
-  if (tid < 192) sm.rest_rows[tid] = 0;
-  if (tid < kWarps) sm.qcnt[tid] = 0;
-  if (tid == 0) {
-    sm.task_next = 0;
-    sm.rest_n = 0;
-  }
-  __syncthreads();
-  if (warp == 0) issue_chunk<KIND>(sm, p, &tmap, 0, lane, cur, end);
+  if (tid < 6) sm.rest_slices[tid] = 0;
   __syncthreads();
 
-  uint32_t phase = 0;  // bit b = parity of buffer b
-  int buf = 0;
+  uint32_t phase = 0;
+  uint32_t qc = 0;  // quads staged in qbuf[warp] (warp-uniform)
   for (;;) {
-    const int c = sm.chunk[buf];
+    if (warp == 0) issue_chunk<KIND>(sm, p, &tmap, lane, cur, end, pending);
+    __syncthreads();
+    const int c = sm.chunk;
     if (c < 0) break;
-    if (warp == 0) issue_chunk<KIND>(sm, p, &tmap, buf ^ 1, lane, cur, end);
-    const bool valid = sm.valid[buf] != 0;
+    const bool valid = sm.valid != 0;
     if constexpr (T::kHalo) {
-      if (valid) compute_halos<KIND>(sm, p, buf, warp, lane);
+      if (valid) compute_halos<KIND>(sm, p, warp, lane);
     }
-    const bool ok = mbar_wait_bounded(&sm.bar[buf], (phase >> buf) & 1u, kWaitLimitNs);
-    phase ^= 1u << buf;
+    const bool ok = mbar_wait_bounded(&sm.bar, phase, kWaitLimitNs);
+    phase ^= 1u;
     if (__syncthreads_or(!ok)) {
-      // A copy did not land within the limit: flag it, give the copies still
-      // in flight (this buffer and the prefetch) one more bounded wait, leave.
+      // the copy did not land within the limit: flag it, give it one more
+      // bounded wait so nothing is in flight into shared memory, and leave
       if (tid == 0) {
         atomicOr(p.err, ERR_TIMEOUT);
-        mbar_wait_bounded(&sm.bar[buf], ((phase >> buf) & 1u) ^ 1u, kWaitLimitNs);
-        if (sm.chunk[buf ^ 1] >= 0)
-          mbar_wait_bounded(&sm.bar[buf ^ 1], (phase >> (buf ^ 1)) & 1u, kWaitLimitNs);
+        mbar_wait_bounded(&sm.bar, phase ^ 1u, kWaitLimitNs);
       }
       __syncthreads();
       return;
     }
     if (valid) {
-      const uint8_t* mb = sm.mat[buf];
+      const uint8_t* mb = sm.mat;
       // ---- pass 1: per z slab (lanes = x): row words by ballot, captured by
-      // lane y; Y faces by shuffles; X-face columns by warp transposes.
+      // lane y; transposed copies for the X faces.
       for (int z = warp; z < 32; z += kWarps) {
         uint32_t r_occ = 0, r_ex = 0, r_ey = 0, r_ez = 0, prev_m = 0;
         for (int y0 = 0; y0 < 32; y0 += 8) {
@@ -440,255 +490,212 @@ __global__ void __launch_bounds__(kThreads, 1)
         sm.ex[o] = r_ex;
         sm.ey[o] = r_ey;
         sm.ez[o] = r_ez;
-        {
-          uint32_t up = __shfl_down_sync(kFull, r_occ, 1), dn = __shfl_up_sync(kFull, r_occ, 1);
-          if (lane == 31) up = sm.halo[3][z];
-          if (lane == 0) dn = sm.halo[2][z];
-          sm.f[2][o] = r_occ & ~up;  // +Y, [z][y]
-          sm.f[3][o] = r_occ & ~dn;  // -Y
-        }
         uint32_t occT = 0, eyT = 0, ezT = 0;
-        if (__any_sync(kFull, r_occ != 0)) {  // an empty slab has no X faces
+        if (__any_sync(kFull, r_occ != 0)) {  // an empty slab needs no transposes
           occT = transpose32(r_occ, lane);
           eyT = transpose32(r_ey, lane);
           ezT = transpose32(r_ez, lane);
+          if (lane == 0) sm.any_solid = 1;
         }
-        uint32_t up = __shfl_down_sync(kFull, occT, 1), dn = __shfl_up_sync(kFull, occT, 1);
-        if (lane == 31) up = sm.halo[1][z];
-        if (lane == 0) dn = sm.halo[0][z];
-        sm.f[0][o] = occT & ~up;  // +X, [z][x] bits y
-        sm.f[1][o] = occT & ~dn;  // -X
+        sm.occt[o] = occT;
         sm.eyt[o] = eyT;
         sm.ezt[o] = ezT;
       }
       __syncthreads();
-      // ---- pass 2: +Z / -Z face masks
-      for (int i = tid; i < 1024; i += kThreads) {
-        const int z = i >> 5, y = i & 31, o = z * kS + y;
-        const uint32_t oc = sm.occ[o];
-        const uint32_t up = z < 31 ? sm.occ[o + kS] : sm.halo[5][y];
-        const uint32_t dn = z > 0 ? sm.occ[o - kS] : sm.halo[4][y];
-        sm.f[4][o] = oc & ~up;
-        sm.f[5][o] = oc & ~dn;
-      }
-      __syncthreads();
-      // ---- pass 3: isolated faces (no same-material face neighbour in the
-      // plane).  Every greedy scan emits them as 1x1 quads and no other quad
-      // touches them, so they are peeled off into registers (thread t holds
-      // the words i = t + 512k, k < 12; a warp holds whole 32-word groups
-      // g = 32*dir + row) and emitted in bulk.
-      uint32_t isow[12];
+      if (sm.any_solid) {
+        // ---- pass 2: isolated faces (no same-material face neighbour in
+        // the plane).  Every greedy scan emits them as 1x1 quads and no other
+        // quad touches them, so they are peeled off into registers: warp w
+        // holds rows v0 .. v0+3 (v0 = 4w) of every direction (lane = slice),
+        // walking the rows in order so the face words of the rows above and
+        // below are carried, not recomputed.
+        const int v0 = warp * 4;
+        uint32_t isow[kGroups];
+        uint32_t lane_iso = 0;
 #pragma unroll
-      for (int k = 0; k < 12; k++) {
-        const int i = tid + k * kThreads;
-        const int d = i >> 10, v = (i >> 5) & 31, sl = i & 31;
-        const int o = word_off(d, sl, v), sv = d < 4 ? kS : 1;
-        const uint32_t* F = sm.f[d];
-        const uint32_t* E = d < 2 ? sm.eyt : sm.ex;
-        const uint32_t* Vv = d < 2 ? sm.ezt : (d < 4 ? sm.ez : sm.ey);
-        const uint32_t fv = F[o];
-        uint32_t w = 0;
-        if (fv) {
-          const uint32_t fu = v > 0 ? F[o - sv] : 0u;
-          const uint32_t fd = v < 31 ? F[o + sv] : 0u;
-          const uint32_t vd = v < 31 ? Vv[o + sv] : 0u;
-          const uint32_t left = fv & E[o] & (fv << 1);
-          const uint32_t upl = fv & Vv[o] & fu;
-          const uint32_t dnl = fv & vd & fd;
-          w = fv & ~(left | (left >> 1) | upl | dnl);
-        }
-        isow[k] = w;
-        const uint32_t n = __reduce_add_sync(kFull, (uint32_t)__popc(w));
-        if (lane == 0) sm.iso_count[i >> 5] = n;
-      }
-      __syncthreads();
-#pragma unroll
-      for (int k = 0; k < 12; k++) {
-        const int i = tid + k * kThreads;
-        const int d = i >> 10, v = (i >> 5) & 31, sl = i & 31;
-        const int o = word_off(d, sl, v);
-        const uint32_t rest = sm.f[d][o] & ~isow[k];
-        sm.f[d][o] = rest;
-        if (rest) {
-          // the first row of a slice to hold non-isolated faces lists the slice
-          if (atomicOr(&sm.rest_rows[d * 32 + sl], 1u << v) == 0u)
-            sm.rest_list[atomicAdd(&sm.rest_n, 1u)] = (uint16_t)(d * 32 + sl);
-        }
-      }
-      if (warp == kWarps - 1) {
-        // exclusive prefix over the 192 word groups (6 per lane) and one
-        // reservation per chunk for all isolated quads
-        uint32_t cnt[6], sum = 0;
-        for (int k = 0; k < 6; k++) {
-          cnt[k] = sm.iso_count[lane * 6 + k];
-          sum += cnt[k];
-        }
-        uint32_t incl = sum;
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t y = __shfl_up_sync(kFull, incl, o);
-          if (lane >= o) incl += y;
-        }
-        uint32_t run = incl - sum;
-        for (int k = 0; k < 6; k++) {
-          sm.iso_off[lane * 6 + k] = run;
-          run += cnt[k];
-        }
-        const uint32_t total = __shfl_sync(kFull, incl, 31);
-        if (lane == 0) {
-          sm.iso_base = total ? atomicAdd(p.count, (unsigned long long)total) : 0ull;
-          sm.chunk_quads += total;
-        }
-      }
-      __syncthreads();
-      const uint64_t chunk_bits = (uint64_t)((p.chunk_id_base + (uint32_t)c) & 0xFFFFFu) << 44;
-      // ---- pass 4a: isolated quads of this warp's 12 groups, 4 groups at a
-      // time so their shuffle chains interleave.  Per group a warp-balanced
-      // expansion: lane j of round k emits the (32k+j)-th set bit of the
-      // group, found by a shuffle binary search over the lanes' prefixes and
-      // __fns inside the owning word.
-#pragma unroll
-      for (int b = 0; b < 3; b++) {
-        uint32_t G[4], ex[4], wv[4];
-        bool any = false;
-#pragma unroll
-        for (int q = 0; q < 4; q++) any |= sm.iso_count[warp + (4 * b + q) * kWarps] != 0;
-        if (!any) continue;
-        uint32_t incl[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          wv[q] = isow[4 * b + q];
-          incl[q] = __popc(wv[q]);
-        }
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
+        for (int d = 0; d < 6; d++) {
+          uint32_t fu = v0 > 0 ? face_row(sm, d, v0 - 1, lane) : 0u;
+          uint32_t fv = face_row(sm, d, v0, lane);
+          uint32_t vv = v_arr(sm, d)[word_off(d, lane, v0)];
+          uint32_t rest = 0;
 #pragma unroll
           for (int q = 0; q < 4; q++) {
-            const uint32_t y = __shfl_up_sync(kFull, incl[q], o);
-            if (lane >= o) incl[q] += y;
+            const int v = v0 + q;
+            const bool last = q == 3 && v0 == 28;
+            const uint32_t fd = last ? 0u : face_row(sm, d, v + 1, lane);
+            const uint32_t vd = last ? 0u : v_arr(sm, d)[word_off(d, lane, v + 1)];
+            const uint32_t w = isolated(fv, fu, fd, e_arr(sm, d)[word_off(d, lane, v)], vv, vd);
+            isow[4 * d + q] = w;
+            lane_iso += __popc(w);
+            rest |= fv & ~w;
+            fu = fv;
+            fv = fd;
+            vv = vd;
           }
+          const uint32_t m = __ballot_sync(kFull, rest != 0u);
+          if (lane == 0 && m) atomicOr(&sm.rest_slices[d], m);
         }
+        const uint32_t total = __reduce_add_sync(kFull, lane_iso);
+        unsigned long long run = 0;
+        if (lane == 0 && total) run = atomicAdd(p.count, (unsigned long long)total);
+        run = __shfl_sync(kFull, run, 0);
+        uint32_t mine = total;
+        const uint64_t chunk_bits = (uint64_t)((p.chunk_id_base + (uint32_t)c) & 0xFFFFFu) << 44;
+        // ---- pass 3: isolated quads of this warp's words, the 4 rows of one
+        // direction at a time (lane = slice).  A warp-balanced expansion over
+        // all set bits of the 4 x 32 words: lane j of round k emits the
+        // (32k+j)-th bit, found by a shuffle binary search over the lanes'
+        // prefixes, then the row from the owning lane's packed running
+        // counts, then __fns inside that word.
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-          ex[q] = incl[q] - __popc(wv[q]);
-          G[q] = __shfl_sync(kFull, incl[q], 31);
-        }
-        uint32_t maxG = 0;
+        for (int dir = 0; dir < 6; dir++) {
+          const uint32_t w0 = isow[4 * dir], w1 = isow[4 * dir + 1], w2 = isow[4 * dir + 2],
+                         w3 = isow[4 * dir + 3];
+          const uint32_t c1 = __popc(w0), c2 = c1 + __popc(w1), c3 = c2 + __popc(w2);
+          const uint32_t n = c3 + __popc(w3);
+          uint32_t incl = n;
 #pragma unroll
-        for (int q = 0; q < 4; q++) maxG = G[q] > maxG ? G[q] : maxG;
-        for (uint32_t k2 = 0; k2 < maxG; k2 += 32) {
-          const uint32_t j = k2 + (uint32_t)lane;
-          int l[4] = {0, 0, 0, 0};
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const uint32_t G = __shfl_sync(kFull, incl, 31);
+          if (G == 0) continue;
+          const uint32_t ex = incl - n;
+          const uint32_t packed = c1 | c2 << 8 | c3 << 16;  // running counts, each <= 96
+          for (uint32_t k2 = 0; k2 < G; k2 += 32) {
+            const uint32_t j = k2 + (uint32_t)lane;
+            int l = 0;
 #pragma unroll
-          for (int step = 16; step >= 1; step >>= 1) {
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-              const uint32_t oc = __shfl_sync(kFull, ex[q], l[q] + step);
-              if (oc <= j) l[q] += step;
+            for (int step = 16; step >= 1; step >>= 1) {
+              const uint32_t oc = __shfl_sync(kFull, ex, l + step);
+              if (oc <= j) l += step;
             }
-          }
-#pragma unroll
-          for (int q = 0; q < 4; q++) {
-            const uint32_t wl = __shfl_sync(kFull, wv[q], l[q]);
-            const uint32_t ol = __shfl_sync(kFull, ex[q], l[q]);
-            if (j < G[q]) {
-              const int g = warp + (4 * b + q) * kWarps;
-              const int dir = g >> 5, v = g & 31;
-              const int u = (int)__fns(wl, 0, (int)(j - ol) + 1);
+            const uint32_t r = j - __shfl_sync(kFull, ex, l);
+            const uint32_t pk = __shfl_sync(kFull, packed, l);
+            const uint32_t x0 = __shfl_sync(kFull, w0, l), x1 = __shfl_sync(kFull, w1, l);
+            const uint32_t x2 = __shfl_sync(kFull, w2, l), x3 = __shfl_sync(kFull, w3, l);
+            if (j < G) {
+              const uint32_t p1 = pk & 0xFFu, p2 = (pk >> 8) & 0xFFu, p3 = pk >> 16;
+              uint32_t wq = x0, rb = 0;
+              int q = 0;
+              if (r >= p1) { wq = x1; rb = p1; q = 1; }
+              if (r >= p2) { wq = x2; rb = p2; q = 2; }
+              if (r >= p3) { wq = x3; rb = p3; q = 3; }
+              const int u = (int)__fns(wq, 0, (int)(r - rb) + 1);
               int x, y, z;
-              face_xyz(dir, l[q], u, v, x, y, z);
+              face_xyz(dir, l, u, v0 + q, x, y, z);
               const uint32_t mat = load_mat<KIND>(mb, x, y, z);
-              const unsigned long long idx = sm.iso_base + sm.iso_off[g] + j;
+              const unsigned long long idx = run + j;
               if (idx < p.cap)
                 p.quads[idx] = chunk_bits | (uint64_t)dir << 41 | (uint64_t)z << 36 | (uint64_t)y << 31 |
                                (uint64_t)x << 26 | mat;
             }
           }
+          run += G;
         }
-      }
-      // ---- pass 4b: greedy on the remaining faces, one warp per slice.
-      // Lane r holds row r of the slice in registers: its faces, their
-      // equality with the -u and -v neighbours, and the bits consumed so far.  Rows are scanned in
-      // order; in a row every maximal run of unconsumed same-material faces
-      // is one quad (Lysenko's left-to-right scan gives exactly these runs);
-      // a quad's height is one ballot over the rows below, and the quads of
-      // one row never interact because their columns are disjoint.
-      uint64_t* qb = sm.qbuf[warp];
-      uint32_t qc = sm.qcnt[warp];  // warp-uniform count of staged quads
-      uint32_t mine = 0;
-      const uint32_t n_tasks = sm.rest_n;
-      for (;;) {
-        uint32_t t = 0;
-        if (lane == 0) t = atomicAdd(&sm.task_next, 1u);
-        t = __shfl_sync(kFull, t, 0);
-        if (t >= n_tasks) break;
-        const int task = sm.rest_list[t];
-        uint32_t rows = sm.rest_rows[task];
-        if (lane == 0) sm.rest_rows[task] = 0;
-        const int dir = task >> 5, sl = task & 31;
-        const int orow = word_off(dir, sl, lane);
-        const uint32_t Fr = sm.f[dir][orow];
-        const uint32_t Er = (dir < 2 ? sm.eyt : sm.ex)[orow];
-        const uint32_t Vr = (dir < 2 ? sm.ezt : (dir < 4 ? sm.ez : sm.ey))[orow];
-        const uint64_t dir_bits = chunk_bits | (uint64_t)dir << 41;
-        uint32_t cons = 0;
-        while (rows) {
-          const int v = __ffs(rows) - 1;
-          rows &= rows - 1;
-          const uint32_t cur = Fr & ~cons;
-          const uint32_t word = __shfl_sync(kFull, cur, v);
-          if (!word) continue;
-          const uint32_t e = __shfl_sync(kFull, Er, v);
-          const uint32_t link = word & e & (word << 1);
-          const uint32_t starts = word & ~link;
-          const uint32_t cnt = __popc(starts);
-          if (qc + cnt > (uint32_t)kQBuf) {
-            if (lane == 0) sm.qcnt[warp] = qc;
-            flush_warp(sm, warp, p, lane);
-            qc = 0;
-          }
-          const uint32_t q0 = qc;
-          // every start lane grows its quad; row r's words come from lane r
-          const bool is_start = (starts >> lane) & 1u;
-          const int w = __ffs(~__funnelshift_rc(link, 0u, (uint32_t)lane + 1u));
-          const uint32_t mask = is_start ? ((2u << (w - 1)) - 1u) << lane : 0u;
-          const uint32_t grow = Fr & Vr;  // faces that continue the row above in material
-          bool active = is_start;
-          int h = 1;
-          for (int r = v + 1; r < 32; r++) {
-            const uint32_t g = __shfl_sync(kFull, grow & ~cons, r);
-            const bool cont = active && (g & mask) == mask;
-            const uint32_t taken = __reduce_or_sync(kFull, cont ? mask : 0u);
-            if (lane == r) cons |= taken;
-            h += cont ? 1 : 0;
-            active = cont;
-            if (!__any_sync(kFull, active)) break;
-          }
-          if (is_start) {
-            int x, y, z;
-            face_xyz(dir, sl, lane, v, x, y, z);
-            const uint32_t mat = load_mat<KIND>(mb, x, y, z);
-            qb[q0 + __popc(starts & lanemask_lt())] = dir_bits | (uint64_t)z << 36 | (uint64_t)y << 31 |
-                                                       (uint64_t)x << 26 | (uint64_t)(w - 1) << 21 |
-                                                       (uint64_t)(h - 1) << 16 | (uint64_t)mat;
-          }
-          qc = q0 + cnt;
-          mine += cnt;
+        __syncthreads();
+        // ---- pass 4: greedy on the remaining faces, one warp per slice.
+        // Lane r holds row r of the slice in registers: its faces (isolated
+        // ones removed again), their equality with the -u and -v neighbours,
+        // and the bits consumed so far.  Rows are scanned in order; in a row
+        // every maximal run of unconsumed same-material faces is one quad
+        // (Lysenko's left-to-right scan gives exactly these runs); a quad's
+        // height is one ballot over the rows below, and the quads of one row
+        // never interact because their columns are disjoint.
+        uint32_t rs[6], pre[6];
+        uint32_t n_tasks = 0;
+#pragma unroll
+        for (int d = 0; d < 6; d++) {
+          rs[d] = sm.rest_slices[d];
+          pre[d] = n_tasks;
+          n_tasks += __popc(rs[d]);
         }
+        uint64_t* qb = sm.qbuf[warp];
+        for (;;) {
+          uint32_t t = 0;
+          if (lane == 0) t = atomicAdd(&sm.task_next, 1u);
+          t = __shfl_sync(kFull, t, 0);
+          if (t >= n_tasks) break;
+          int dir = 0;
+          uint32_t before = 0, smask = rs[0];
+#pragma unroll
+          for (int d = 1; d < 6; d++) {
+            if (t >= pre[d]) {
+              dir = d;
+              before = pre[d];
+              smask = rs[d];
+            }
+          }
+          const int sl = (int)__fns(smask, 0, (int)(t - before) + 1);
+          const int orow = word_off(dir, sl, lane);
+          const uint32_t F0 = face_col(sm, dir, sl, lane);
+          const uint32_t Er = e_arr(sm, dir)[orow];
+          const uint32_t Vr = v_arr(sm, dir)[orow];
+          uint32_t fu = __shfl_up_sync(kFull, F0, 1), fd = __shfl_down_sync(kFull, F0, 1);
+          uint32_t vd = __shfl_down_sync(kFull, Vr, 1);
+          if (lane == 0) fu = 0;
+          if (lane == 31) fd = vd = 0;
+          const uint32_t Fr = F0 & ~isolated(F0, fu, fd, Er, Vr, vd);
+          uint32_t rows = __ballot_sync(kFull, Fr != 0);
+          const uint64_t dir_bits = chunk_bits | (uint64_t)dir << 41;
+          uint32_t cons = 0;
+          while (rows) {
+            const int v = __ffs(rows) - 1;
+            rows &= rows - 1;
+            const uint32_t cur = Fr & ~cons;
+            const uint32_t word = __shfl_sync(kFull, cur, v);
+            if (!word) continue;
+            const uint32_t e = __shfl_sync(kFull, Er, v);
+            const uint32_t link = word & e & (word << 1);
+            const uint32_t starts = word & ~link;
+            const uint32_t cnt = __popc(starts);
+            if (qc + cnt > (uint32_t)kQBuf) {
+              flush_warp(sm, warp, p, lane, qc);
+              qc = 0;
+            }
+            const uint32_t q0 = qc;
+            // every start lane grows its quad; row r's words come from lane r
+            const bool is_start = (starts >> lane) & 1u;
+            const int w = __ffs(~__funnelshift_rc(link, 0u, (uint32_t)lane + 1u));
+            const uint32_t mask = is_start ? ((2u << (w - 1)) - 1u) << lane : 0u;
+            const uint32_t grow = Fr & Vr;  // faces that continue the row above in material
+            bool active = is_start;
+            int h = 1;
+            for (int r = v + 1; r < 32; r++) {
+              const uint32_t g = __shfl_sync(kFull, grow & ~cons, r);
+              const bool cont = active && (g & mask) == mask;
+              const uint32_t taken = __reduce_or_sync(kFull, cont ? mask : 0u);
+              if (lane == r) cons |= taken;
+              h += cont ? 1 : 0;
+              active = cont;
+              if (!__any_sync(kFull, active)) break;
+            }
+            if (is_start) {
+              int x, y, z;
+              face_xyz(dir, sl, lane, v, x, y, z);
+              const uint32_t mat = load_mat<KIND>(mb, x, y, z);
+              qb[q0 + __popc(starts & lanemask_lt())] = dir_bits | (uint64_t)z << 36 | (uint64_t)y << 31 |
+                                                         (uint64_t)x << 26 | (uint64_t)(w - 1) << 21 |
+                                                         (uint64_t)(h - 1) << 16 | (uint64_t)mat;
+            }
+            qc = q0 + cnt;
+            mine += cnt;
+          }
+        }
+        if (p.chunk_counts && lane == 0 && mine) atomicAdd(&sm.chunk_quads, mine);
       }
-      if (lane == 0) sm.qcnt[warp] = qc;
-      __syncwarp();
-      if (p.chunk_counts && lane == 0 && mine) atomicAdd(&sm.chunk_quads, mine);
     }
     __syncthreads();
     if (tid == 0) {
       if (p.chunk_counts) p.chunk_counts[c] = valid ? sm.chunk_quads : 0u;
       sm.chunk_quads = 0;
       sm.task_next = 0;
-      sm.rest_n = 0;
+      sm.any_solid = 0;
     }
-    buf ^= 1;
+    if (tid < 6) sm.rest_slices[tid] = 0;
   }
-  flush_warp(sm, warp, p, lane);
+  flush_warp(sm, warp, p, lane, qc);
 }
 
 // --------------------------------------------------------------- host side
@@ -729,6 +736,8 @@ meso_status launch_kind(meso_ctx* ctx, const MeshParams& base, const CUtensorMap
   static bool attr_set[64] = {false};
   if (!attr_set[ctx->device & 63]) {
     MESO_CUDA_TRY(cudaFuncSetAttribute(mesh_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MESO_CUDA_TRY(cudaFuncSetAttribute(mesh_kernel<KIND>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       (int)cudaSharedmemCarveoutMaxShared));
     attr_set[ctx->device & 63] = true;
   }
   constexpr bool kCoords3 = KindTraits<KIND>::kGrid || KindTraits<KIND>::kBrick;
@@ -750,7 +759,7 @@ meso_status launch_kind(meso_ctx* ctx, const MeshParams& base, const CUtensorMap
   }
   MeshParams p = base;
   p.use_queue = 1;
-  uint32_t grid = ctx->sm_count * (ctx->tuning.mesh_ctas_per_sm ? ctx->tuning.mesh_ctas_per_sm : 1);
+  uint32_t grid = ctx->sm_count * (ctx->tuning.mesh_ctas_per_sm ? ctx->tuning.mesh_ctas_per_sm : 2);
   const uint32_t per = p.per_ticket ? p.per_ticket : 1;
   const uint32_t need = (n_chunks + per - 1) / per;
   if (grid > need) grid = need;
