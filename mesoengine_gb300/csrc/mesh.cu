@@ -18,9 +18,11 @@
 //     ballots: occupancy and material-equality with the -x, -y and -z
 //     neighbour, plus warp-transposed copies (bits over y) for the X faces;
 //     face masks occ & ~shift(occ) are recomputed from these where needed;
-//  3. isolated faces (no same-material face neighbour in their plane) are
-//     peeled off in registers and emitted as 1x1 quads by a warp-balanced
-//     expansion, one output reservation per warp and chunk;
+//  3. faces whose quad cannot depend on the scan order are peeled off
+//     first: isolated faces (no same-material face neighbour in their plane)
+//     become 1x1 quads through a warp-balanced expansion with one output
+//     reservation per warp and chunk, and two-face components become 2x1 or
+//     1x2 quads at the start of their slice's greedy;
 //  4. greedy: warp = slice with non-isolated faces, lane = row; rows are
 //     scanned with run-length bit tricks (Lysenko's order: first unconsumed
 //     face, widen along u while the material matches, grow along v while the
@@ -504,9 +506,10 @@ __global__ void __launch_bounds__(kThreads, 2)
       __syncthreads();
       if (sm.any_solid) {
         // ---- pass 2: isolated faces (no same-material face neighbour in
-        // the plane).  Every greedy scan emits them as 1x1 quads and no other
-        // quad touches them, so they are peeled off into registers: warp w
-        // holds rows v0 .. v0+3 (v0 = 4w) of every direction (lane = slice),
+        // the plane).  Quads never leave a component of same-material,
+        // edge-adjacent faces, so these are 1x1 quads whatever the greedy
+        // does elsewhere: they are peeled off into registers.  Warp w holds
+        // rows v0 .. v0+3 (v0 = 4w) of every direction (lane = slice),
         // walking the rows in order so the face words of the rows above and
         // below are carried, not recomputed.
         const int v0 = warp * 4;
@@ -547,10 +550,12 @@ __global__ void __launch_bounds__(kThreads, 2)
         // (32k+j)-th bit, found by a shuffle binary search over the lanes'
         // prefixes, then the row from the owning lane's packed running
         // counts, then __fns inside that word.
-#pragma unroll
+#pragma unroll 1
         for (int dir = 0; dir < 6; dir++) {
-          const uint32_t w0 = isow[4 * dir], w1 = isow[4 * dir + 1], w2 = isow[4 * dir + 2],
-                         w3 = isow[4 * dir + 3];
+          // this direction's words are isow[0..3]; the rest shift down by 4
+          const uint32_t w0 = isow[0], w1 = isow[1], w2 = isow[2], w3 = isow[3];
+#pragma unroll
+          for (int i = 0; i + 4 < kGroups; i++) isow[i] = isow[i + 4];
           const uint32_t c1 = __popc(w0), c2 = c1 + __popc(w1), c3 = c2 + __popc(w2);
           const uint32_t n = c3 + __popc(w3);
           uint32_t incl = n;
@@ -636,7 +641,48 @@ __global__ void __launch_bounds__(kThreads, 2)
           uint32_t vd = __shfl_down_sync(kFull, Vr, 1);
           if (lane == 0) fu = 0;
           if (lane == 31) fd = vd = 0;
-          const uint32_t Fr = F0 & ~isolated(F0, fu, fd, Er, Vr, vd);
+          // the faces pass 2 left: not isolated and not in a domino
+          const uint32_t hl = F0 & Er & (F0 << 1), hh = hl | (hl >> 1);
+          const uint32_t ul = F0 & Vr & fu, dl = F0 & vd & fd, vl = ul | dl;
+          const uint32_t hd = hl & ~(hl << 1) & ~(hl >> 1) & ~vl & ~(vl << 1);
+          uint32_t hn = __shfl_down_sync(kFull, hh, 1), dn = __shfl_down_sync(kFull, dl, 1);
+          if (lane == 31) hn = dn = 0;
+          const uint32_t vdt = dl & ~hh & ~ul & ~hn & ~dn;
+          uint32_t vdb = __shfl_up_sync(kFull, vdt, 1);
+          if (lane == 0) vdb = 0;
+          const uint32_t Fr = F0 & (hh | vl) & ~(hd | (hd >> 1) | vdt | vdb);
+          {
+            // two-face components first: a 2x1 or 1x2 quad whatever the
+            // scan order (origins hd >> 1: 2 wide, vdt: 2 high; lane = row)
+            uint32_t ho = hd >> 1, vo = vdt;
+            while (__any_sync(kFull, (ho | vo) != 0u)) {
+              const bool horiz = ho != 0u;
+              const uint32_t act = __ballot_sync(kFull, (ho | vo) != 0u);
+              const uint32_t n = __popc(act);
+              if (qc + n > (uint32_t)kQBuf) {
+                flush_warp(sm, warp, p, lane, qc);
+                qc = 0;
+              }
+              if (ho | vo) {
+                uint32_t u;
+                if (horiz) {
+                  u = __ffs(ho) - 1;
+                  ho &= ho - 1u;
+                } else {
+                  u = __ffs(vo) - 1;
+                  vo &= vo - 1u;
+                }
+                int x, y, z;
+                face_xyz(dir, sl, (int)u, lane, x, y, z);
+                const uint32_t mat = load_mat<KIND>(mb, x, y, z);
+                qb[qc + __popc(act & lanemask_lt())] =
+                    chunk_bits | (uint64_t)dir << 41 | (uint64_t)z << 36 | (uint64_t)y << 31 | (uint64_t)x << 26 |
+                    (uint64_t)(horiz ? 1u : 0u) << 21 | (uint64_t)(horiz ? 0u : 1u) << 16 | (uint64_t)mat;
+              }
+              qc += n;
+              mine += n;
+            }
+          }
           uint32_t rows = __ballot_sync(kFull, Fr != 0);
           const uint64_t dir_bits = chunk_bits | (uint64_t)dir << 41;
           uint32_t cons = 0;
