@@ -287,6 +287,38 @@ __device__ __forceinline__ void issue_chunk(MeshSmem& sm, const MeshParams& p, c
   }
 }
 
+// The chunk the next issue_chunk will take (lane 0 of warp 0), so its data
+// can be prefetched into L2 while this chunk is meshed.  Only the index (and
+// for grid sources the coordinates) is loaded here; prefetch_chunk uses it
+// later, after the load has landed.  a < 0: nothing to prefetch.
+template <int KIND>
+__device__ __forceinline__ void next_chunk(const MeshParams& p, uint32_t cur, uint32_t end, uint32_t pending,
+                                           int32_t& a, int32_t& b, int32_t& c) {
+  using T = KindTraits<KIND>;
+  a = -1;
+  const uint32_t n = p.use_queue ? (cur < end ? cur : pending) : cur;
+  if (n >= p.n_chunks || T::kBrick) return;
+  if constexpr (T::kGrid) {
+    a = p.coords[3 * n];
+    b = p.coords[3 * n + 1];
+    c = p.coords[3 * n + 2];
+  } else {
+    a = p.coords ? p.coords[n] : (int32_t)n;
+  }
+}
+
+template <int KIND>
+__device__ __forceinline__ void prefetch_chunk(const MeshParams& p, const CUtensorMap* tmap, int32_t a, int32_t b,
+                                               int32_t c) {
+  using T = KindTraits<KIND>;
+  if (a < 0) return;
+  if constexpr (T::kGrid) {
+    if (b >= 0 && c >= 0 && a < p.nx / 32 && b < p.ny / 32 && c < p.nz / 32) tma_prefetch_3d(tmap, a * 32, b * 32, c * 32);
+  } else if constexpr (!T::kBrick) {
+    if (!p.coords || a < p.nx) bulk_prefetch_l2(p.data + (size_t)a * 32768u * T::kElem, 32768u * T::kElem);
+  }
+}
+
 template <int KIND>
 __device__ __forceinline__ void compute_halos(MeshSmem& sm, const MeshParams& p, int warp, int lane) {
   const int X = sm.coord[0] * 32, Y = sm.coord[1] * 32, Z = sm.coord[2] * 32;
@@ -447,63 +479,76 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
     if (valid) {
       const uint8_t* mb = sm.mat;
-      // ---- pass 1: per z slab (lanes = x): row words by ballot, captured by
-      // lane y; transposed copies for the X faces.
-      for (int z = warp; z < 32; z += kWarps) {
-        uint32_t r_occ = 0, r_ex = 0, r_ey = 0, r_ez = 0, prev_m = 0;
+      // ---- pass 1: warp w builds slabs z0 .. z0+3 (z0 = 4w; lanes = x),
+      // 8 rows of the 4 slabs at a time, so the previous slab's materials
+      // are still in registers for the -z equality.  Row words come from
+      // ballots and are stored by lane 0; the transposed copies for the X
+      // faces are made at the end.
+      {
+        const int z0 = warp * 4;
+        uint32_t prev_m[4] = {0, 0, 0, 0};  // row y0-1 of each slab
+#pragma unroll 1
         for (int y0 = 0; y0 < 32; y0 += 8) {
-          if (rows8_empty<KIND>(mb, y0, z, lane)) {
-            prev_m = 0;  // row y0+7 is empty; nothing to capture
-            continue;
-          }
-          // 8 rows at a time: all loads first, then the votes
-          const int dl = lane - y0;  // row captured by this lane, if in 0..7
-          uint32_t m[8], occw[8];
+          uint32_t mp[8];  // rows y0 .. y0+7 of the slab below
 #pragma unroll
-          for (int k = 0; k < 8; k++) m[k] = load_mat<KIND>(mb, lane, y0 + k, z);
-          uint32_t any = 0;
+          for (int k = 0; k < 8; k++) mp[k] = z0 > 0 ? load_mat<KIND>(mb, lane, y0 + k, z0 - 1) : 0u;
 #pragma unroll
-          for (int k = 0; k < 8; k++) {
-            occw[k] = __ballot_sync(kFull, m[k] != 0);
-            any |= occw[k];
-            if (dl == k) r_occ = occw[k];
-          }
-          if (any) {  // equality bits only matter on solid voxels
-            uint32_t mz[8];
+          for (int j = 0; j < 4; j++) {
+            const int z = z0 + j, o = z * kS + y0;
+            if (rows8_empty<KIND>(mb, y0, z, lane)) {
+              if (lane < 8) {
+                sm.occ[o + lane] = 0;
+                sm.ex[o + lane] = 0;
+                sm.ey[o + lane] = 0;
+                sm.ez[o + lane] = 0;
+              }
 #pragma unroll
-            for (int k = 0; k < 8; k++) mz[k] = z > 0 ? load_mat<KIND>(mb, lane, y0 + k, z - 1) : 0u;
+              for (int k = 0; k < 8; k++) mp[k] = 0;
+              prev_m[j] = 0;
+              continue;
+            }
+            uint32_t m[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) m[k] = load_mat<KIND>(mb, lane, y0 + k, z);
 #pragma unroll
             for (int k = 0; k < 8; k++) {
               const uint32_t ml = __shfl_up_sync(kFull, m[k], 1);
+              const uint32_t occw = __ballot_sync(kFull, m[k] != 0);
               const uint32_t exw = __ballot_sync(kFull, m[k] == ml);
-              const uint32_t eyw = __ballot_sync(kFull, m[k] == (k ? m[k - 1] : prev_m));
-              const uint32_t ezw = __ballot_sync(kFull, m[k] == mz[k]);
-              if (dl == k) {
-                r_ex = exw;
-                r_ey = eyw;
-                r_ez = ezw;
+              const uint32_t eyw = __ballot_sync(kFull, m[k] == (k ? m[k - 1] : prev_m[j]));
+              const uint32_t ezw = __ballot_sync(kFull, m[k] == mp[k]);
+              if (lane == 0) {
+                sm.occ[o + k] = occw;
+                sm.ex[o + k] = exw;
+                sm.ey[o + k] = eyw;
+                sm.ez[o + k] = ezw;
               }
             }
+            prev_m[j] = m[7];
+#pragma unroll
+            for (int k = 0; k < 8; k++) mp[k] = m[k];
           }
-          prev_m = m[7];
         }
-        const int o = z * kS + lane;
-        sm.occ[o] = r_occ;
-        sm.ex[o] = r_ex;
-        sm.ey[o] = r_ey;
-        sm.ez[o] = r_ez;
-        uint32_t occT = 0, eyT = 0, ezT = 0;
-        if (__any_sync(kFull, r_occ != 0)) {  // an empty slab needs no transposes
-          occT = transpose32(r_occ, lane);
-          eyT = transpose32(r_ey, lane);
-          ezT = transpose32(r_ez, lane);
-          if (lane == 0) sm.any_solid = 1;
+        __syncwarp();
+#pragma unroll 1
+        for (int j = 0; j < 4; j++) {
+          const int o = (z0 + j) * kS + lane;
+          const uint32_t r_occ = sm.occ[o];
+          uint32_t occT = 0, eyT = 0, ezT = 0;
+          if (__any_sync(kFull, r_occ != 0)) {  // an empty slab needs no transposes
+            occT = transpose32(r_occ, lane);
+            eyT = transpose32(sm.ey[o], lane);
+            ezT = transpose32(sm.ez[o], lane);
+            if (lane == 0) sm.any_solid = 1;
+          }
+          sm.occt[o] = occT;
+          sm.eyt[o] = eyT;
+          sm.ezt[o] = ezT;
         }
-        sm.occt[o] = occT;
-        sm.eyt[o] = eyT;
-        sm.ezt[o] = ezT;
       }
       __syncthreads();
+      int32_t pf_a = -1, pf_b = 0, pf_c = 0;
+      if (tid == 0) next_chunk<KIND>(p, cur, end, pending, pf_a, pf_b, pf_c);
       if (sm.any_solid) {
         // ---- pass 2: isolated faces (no same-material face neighbour in
         // the plane).  Quads never leave a component of same-material,
@@ -599,6 +644,7 @@ __global__ void __launch_bounds__(kThreads, 2)
           }
           run += G;
         }
+        if (tid == 0) prefetch_chunk<KIND>(p, &tmap, pf_a, pf_b, pf_c);
         __syncthreads();
         // ---- pass 4: greedy on the remaining faces, one warp per slice.
         // Lane r holds row r of the slice in registers: its faces (isolated
