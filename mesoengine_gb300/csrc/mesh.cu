@@ -132,6 +132,19 @@ __device__ __forceinline__ uint32_t load_mat(const uint8_t* buf, int x, int y, i
   }
 }
 
+// Material at chunk-local linear index lin = x + 32 y + 1024 z.
+template <int KIND>
+__device__ __forceinline__ uint32_t load_mat_lin(const uint8_t* buf, uint32_t lin) {
+  using T = KindTraits<KIND>;
+  if constexpr (T::kBrick) {
+    return load_mat<KIND>(buf, (int)(lin & 31u), (int)((lin >> 5) & 31u), (int)(lin >> 10));
+  } else if constexpr (T::kElem == 2) {
+    return reinterpret_cast<const uint16_t*>(buf)[lin];
+  } else {
+    return buf[lin];
+  }
+}
+
 // True iff the 8 rows y0..y0+7 (y0 % 8 == 0) of slab z are all empty: one
 // 16-byte (8-byte for uint8) shared load per lane covers the 256 voxels.
 template <int KIND>
@@ -613,6 +626,11 @@ __global__ void __launch_bounds__(kThreads, 2)
           if (G == 0) continue;
           const uint32_t ex = incl - n;
           const uint32_t packed = c1 | c2 << 8 | c3 << 16;  // running counts, each <= 96
+          // bit offsets of slice, column and row in the linear voxel index
+          const int sh_s = dir < 2 ? 0 : (dir < 4 ? 5 : 10);
+          const int sh_u = dir < 2 ? 5 : 0;
+          const int sh_v = dir < 4 ? 10 : 5;
+          const uint64_t dir_bits = chunk_bits | (uint64_t)dir << 41;
           for (uint32_t k2 = 0; k2 < G; k2 += 32) {
             const uint32_t j = k2 + (uint32_t)lane;
             int l = 0;
@@ -632,14 +650,11 @@ __global__ void __launch_bounds__(kThreads, 2)
               if (r >= p1) { wq = x1; rb = p1; q = 1; }
               if (r >= p2) { wq = x2; rb = p2; q = 2; }
               if (r >= p3) { wq = x3; rb = p3; q = 3; }
-              const int u = (int)__fns(wq, 0, (int)(r - rb) + 1);
-              int x, y, z;
-              face_xyz(dir, l, u, v0 + q, x, y, z);
-              const uint32_t mat = load_mat<KIND>(mb, x, y, z);
+              const uint32_t u = __fns(wq, 0, (int)(r - rb) + 1);
+              const uint32_t lin = (uint32_t)l << sh_s | u << sh_u | (uint32_t)(v0 + q) << sh_v;
+              const uint32_t mat = load_mat_lin<KIND>(mb, lin);
               const unsigned long long idx = run + j;
-              if (idx < p.cap)
-                p.quads[idx] = chunk_bits | (uint64_t)dir << 41 | (uint64_t)z << 36 | (uint64_t)y << 31 |
-                               (uint64_t)x << 26 | mat;
+              if (idx < p.cap) p.quads[idx] = dir_bits | (uint64_t)lin << 26 | mat;
             }
           }
           run += G;
