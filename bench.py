@@ -249,7 +249,35 @@ def bench_mesh(ctx, meso, steps, warmup):
     vox = MESH_CHUNKS * 32768
     algo = MESH_CHUNKS * 65536 + 8 * quads
     return {"ms": ms, "ms_plain": ms_plain, "quads": quads, "gvox_s": vox / (ms * 1e6),
-            "gvox_s_plain": vox / (ms_plain * 1e6), "algo_bytes": algo}
+            "gvox_s_plain": vox / (ms_plain * 1e6), "algo_bytes": algo, "data": data, "qbuf": qbuf}
+
+
+def cpu_mesh_baseline(m, n_single=512):
+    """Oracle mesher on the host cores: all threads over the whole batched
+    workload (checked bit for bit against the GPU's quads), one thread over
+    the first n_single chunks."""
+    import ctypes
+    import oracle
+    data = np.ascontiguousarray(m["data"].download(np.uint16).reshape(MESH_CHUNKS, 32, 32, 32))
+    gq = np.sort(m["qbuf"].download(np.uint64, count=m["quads"]))
+    src = oracle._source(oracle.SRC_CHUNKS_U16, data)
+    coords = np.zeros((MESH_CHUNKS, 3), np.int32)
+    coords[:, 0] = np.arange(MESH_CHUNKS)
+    out = np.zeros(len(gq) + 1, np.uint64)
+    threads = oracle.hardware_threads()
+    t0 = time.perf_counter()
+    total = int(oracle.lib().mo_mesh_chunks_mt(ctypes.byref(src), oracle._ptr(coords), MESH_CHUNKS, threads,
+                                                 oracle._ptr(out), out.size))
+    dt = time.perf_counter() - t0
+    parity = total == len(gq) and bool(np.array_equal(out[:total], gq))
+    t0 = time.perf_counter()
+    oracle.lib().mo_mesh_chunks_mt(ctypes.byref(src), oracle._ptr(coords), n_single, 1, oracle._ptr(out), out.size)
+    dt1 = time.perf_counter() - t0
+    return {"value": round(MESH_CHUNKS * 32768 / dt / 1e9, 4), "unit": "Gvox/s", "cores": threads, "kind": "port",
+            "sample": f"all {MESH_CHUNKS} chunks, {dt:.2f} s",
+            "single_thread": {"value": round(n_single * 32768 / dt1 / 1e9, 5), "unit": "Gvox/s", "cores": 1,
+                              "sample": f"the first {n_single} chunks, {dt1:.2f} s"},
+            "parity_bit_exact": parity}
 
 
 def poisson_arrivals(rate, seconds, seed):
@@ -448,8 +476,14 @@ def cpu_baseline_port(meso, ctx, r):
     h = oracle.raymarch(bm, ocam, nthreads=threads)
     dt = time.perf_counter() - t0
     parity = bool(np.array_equal(h.view(np.uint8), r["hits"].view(np.uint8)))
+    rows, row0 = FRAME_H // 8, (FRAME_H - FRAME_H // 8) // 2
+    t0 = time.perf_counter()
+    h1 = oracle.raymarch_rows(bm, ocam, row0, rows, nthreads=1)
+    dt1 = time.perf_counter() - t0
     return {"value": count_rays(h) / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
             "sample": f"the full {FRAME_W}x{FRAME_H} frame (primary + shadow), {dt:.2f} s",
+            "single_thread": {"value": round(count_rays(h1) / dt1 / 1e6, 3), "unit": "Mrays/s", "cores": 1,
+                              "sample": f"rows {row0}-{row0 + rows - 1} of the frame, {dt1:.2f} s"},
             "parity_full_frame_bit_exact": parity}
 
 
@@ -511,6 +545,8 @@ def run_ours(args, world, rank, local, dist):
                          "frac": round(ach / hbm, 4), "algorithmic_bytes_per_launch": m["algo_bytes"],
                          "traffic": ncu_traffic("mesh_kernel<CHUNKS_U16>"), "kernel": "mesh_kernel<CHUNKS_U16>"},
         }
+        if not args.skip_cpu:
+            line["mesh"]["cpu_baseline"] = cpu_mesh_baseline(m)
     if rank == 0 and not args.skip_serve:
         line["served"] = bench_serve_render(ctx, meso, args.serve_seconds)
         line["served_edit"] = bench_serve_edit(ctx, meso, args.serve_seconds)
