@@ -523,7 +523,7 @@ def run_ours(args, world, rank, local, dist):
         "clocks": clk,
         "e2e": {"value": round(r["rays"] / (r["e2e_ms"] * 1e3), 2), "unit": "Mrays/s",
                 "h2d_bytes_per_step": 72, "d2h_bytes_per_step": FRAME_W * FRAME_H * 24,
-                "api": "meso_raymarch_host (pinned host hit buffer)"},
+                "api": "meso_raymarch_host (camera from host memory; the kernel writes the hits into a page-locked host buffer over the CPU-GPU link)"},
         "gpu_launches": int(r["launches"]),
         "roofline": {
             "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",

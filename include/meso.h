@@ -243,7 +243,11 @@ meso_status meso_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, const 
 meso_status meso_raymarch_per_view(meso_ctx* ctx, const meso_scene* const* scenes,
                                    const meso_camera* h_cams, uint32_t n_views, const float light[3],
                                    uint32_t flags, meso_hit* d_hits, void* stream);
-/* Host-buffer form: hits are copied back into h_hits. */
+/* Host-buffer form: the hits land in h_hits when the call returns.  When
+ * h_hits is page-locked and device-mapped (meso_host_alloc_pinned, or
+ * cudaHostRegister with mapping), the kernel writes the hits straight into
+ * it, overlapped with the tracing; otherwise they go through a device buffer
+ * and one copy. */
 meso_status meso_raymarch_host(meso_ctx* ctx, const meso_scene* scene, const meso_camera* h_cam,
                                const float light[3], uint32_t flags, meso_hit* h_hits);
 

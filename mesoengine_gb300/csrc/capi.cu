@@ -409,6 +409,20 @@ meso_status meso_raymarch_host(meso_ctx* ctx, const meso_scene* scene, const mes
   if (!ctx || !scene || !cam || !h_hits) return fail(MESO_ERR_INVALID_ARG, "raymarch_host: null argument");
   cudaStream_t st = ctx->stream;
   const size_t n = (size_t)cam->width * cam->height;
+  // Page-locked, device-mapped output: the kernel stores the hits straight
+  // into host memory over the CPU-GPU link, overlapped with the tracing, so
+  // there is no separate copy.  Pageable output: device buffer, one copy.
+  cudaPointerAttributes pa;
+  const bool mapped = cudaPointerGetAttributes(&pa, h_hits) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+                      pa.devicePointer != nullptr;
+  if (!mapped) cudaGetLastError();
+  if (mapped) {
+    meso_status rc = launch_raymarch(ctx, &scene, cam, 1, light, flags, static_cast<meso_hit*>(pa.devicePointer), st,
+                                     nullptr, 0);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (rc == MESO_OK && e != cudaSuccess) rc = cuda_fail(e, "raymarch_host");
+    return rc;
+  }
   meso_hit* d = nullptr;
   MESO_CUDA_TRY(cudaMallocAsync(&d, n * sizeof(meso_hit), st));
   meso_status rc = launch_raymarch(ctx, &scene, cam, 1, light, flags, d, st, nullptr, 0);

@@ -113,6 +113,22 @@ def test_raymarch_host_entry(ctx, small):
     assert_hits_equal(ctx.raymarch_host(scene, cam), oracle.raymarch(bm, ocam))
 
 
+@pytest.mark.parametrize("height", [1, 389, 1100])
+def test_raymarch_host_pinned_direct(ctx, small, height):
+    # a page-locked output is written by the kernel directly (no device
+    # buffer, no copy); every byte of it must be overwritten
+    t, scene, bm = small
+    w = 40
+    cam = meso.camera((-20.0, 150.0, 90.0), (64.0, 64.0, 10.0), w, height)
+    ocam = oracle.camera((-20.0, 150.0, 90.0), (64.0, 64.0, 10.0), w, height)
+    buf = ctx.pinned(w * height * meso.HIT_DTYPE.itemsize)
+    buf.view(np.uint8)[:] = 0xAB
+    ctx.raymarch_host(scene, cam, out_ptr=buf.ptr)
+    got = buf.view(meso.HIT_DTYPE, w * height).copy()
+    buf.free()
+    assert_hits_equal(got, oracle.raymarch(bm, ocam))
+
+
 def test_matches_golden_fixture(ctx, small):
     import os
     golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
