@@ -139,7 +139,8 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
           n_fetch++;
           n_brick += p != MESO_EMPTY_BRICK;
         }
-        if (p != MESO_EMPTY_BRICK) break;
+        // the next boundary time is computed while the pointer load is in
+        // flight; an occupied brick recomputes its times from scratch
         nbx += a0 ? 8 * sx : 0;
         nby += a1 ? 8 * sy : 0;
         nbz += a2 ? 8 * sz : 0;
@@ -150,6 +151,7 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
         tx = a0 ? tn : tx;
         ty = a1 ? tn : ty;
         tz = a2 ? tn : tz;
+        if (p != MESO_EMPTY_BRICK) break;
       }
       ea = a;
       if (out || p == MESO_EMPTY_BRICK) break;
@@ -189,6 +191,9 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
       vx += a0 ? sx : 0;
       vy += a1 ? sy : 0;
       vz += a2 ? sz : 0;
+      // next z layer's word, in flight during the bookkeeping below (on a
+      // brick exit it wraps within this brick's 8 words and is unused)
+      if (a2) w = __ldg(occ + (vz & 7));
       const int c = a0 ? vx : (a1 ? vy : vz);
       const int cb = a0 ? Bx : (a1 ? By : Bz);
       exit_brick = (c >> 3) != cb;
@@ -210,7 +215,6 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
       tx = a0 ? tn : tx;
       ty = a1 ? tn : ty;
       tz = a2 ? tn : tz;
-      if (a2) w = __ldg(occ + (vz & 7));
       if (cs + fs > cap) {
         left = true;
         break;
