@@ -9,8 +9,6 @@
 #include "meso_internal.h"
 
 namespace meso {
-meso_status scene_alloc(meso_ctx*, int32_t, int32_t, int32_t, uint64_t, meso_scene**);
-void scene_release(meso_ctx*, meso_scene*);
 
 namespace {
 
@@ -324,6 +322,15 @@ meso_status meso_scene_load(meso_ctx* ctx, const char* path, uint64_t spare, mes
   if (e != cudaSuccess) {
     scene_release(ctx, s);
     return cuda_fail(e, "scene_load: upload");
+  }
+  meso_status rc = rebuild_macro(ctx, s, nullptr, 0, ctx->stream);
+  if (rc == MESO_OK) {
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "scene_load: macro map");
+  }
+  if (rc != MESO_OK) {
+    scene_release(ctx, s);
+    return rc;
   }
   s->live_bricks_host = n;
   *out = s;

@@ -75,6 +75,9 @@ struct meso_scene {
   uint32_t* d_ptr = nullptr;   // brick pointers
   uint64_t* d_occ = nullptr;   // 8 words per slot
   uint16_t* d_mat = nullptr;   // 512 per slot
+  // one byte per 4x4x4-brick cell (a 32^3 chunk): nonzero iff a brick of the
+  // cell is occupied; lets a ray cross an empty cell in one jump
+  uint8_t* d_macro = nullptr;
   uint64_t capacity = 0;       // pool slots
   // allocator state (device): [0] bump (slots ever used), [1] free-stack top
   int64_t* d_alloc = nullptr;
@@ -88,6 +91,7 @@ namespace meso {
 inline uint64_t n_bricks_of(const meso_scene* s) {
   return (uint64_t)s->bx * (uint64_t)s->by * (uint64_t)s->bz;
 }
+inline uint64_t n_macro_of(const meso_scene* s) { return n_bricks_of(s) / 64; }
 
 inline cudaStream_t pick_stream(meso_ctx* ctx, void* s) {
   return s ? (cudaStream_t)s : ctx->stream;
@@ -97,6 +101,9 @@ inline cudaStream_t pick_stream(meso_ctx* ctx, void* s) {
 meso_status scene_alloc(meso_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, uint64_t capacity,
                         meso_scene** out);
 void scene_release(meso_ctx* ctx, meso_scene* s);
+// Recomputes the macro-cell map of a scene from its pointer grid: all cells,
+// or the n cells listed in d_cells (linear macro-cell indices).
+meso_status rebuild_macro(meso_ctx* ctx, meso_scene* s, const uint32_t* d_cells, uint32_t n, cudaStream_t st);
 
 // Kernel launchers (defined in the .cu files).
 meso_status launch_mesh(meso_ctx* ctx, const meso_mesh_source* src, const int32_t* d_coords,

@@ -24,6 +24,7 @@ struct RayView {
   const uint32_t* ptr;
   const uint64_t* occ;
   const uint16_t* mat;
+  const uint8_t* macro;  // per 4x4x4-brick cell: nonzero iff a brick of it is occupied
   int32_t nx, ny, nz;
   int32_t cam_chunk[3];
   float o[3];
@@ -72,6 +73,26 @@ __device__ __forceinline__ float bound_time(int b, float o, float inv) {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// Brick steps the two-level DDA takes along axis c (sign s, brick B, next
+// brick boundary nb) while it crosses the empty 4x4x4-brick cell that B lies
+// in, up to the step that leaves the cell through axis aE at time tE.  The
+// DDA takes its boundary events in (time, axis x<y<z) order and the events of
+// one axis come at strictly increasing times, so the steps along c are its
+// interior boundaries that precede (tE, aE) in that order; along aE they are
+// all interior boundaries plus the exit itself.
+__device__ __forceinline__ int cell_steps(int c, int aE, int s, int B, int nb, float o, float inv, float tE) {
+  if (s == 0) return 0;
+  const int inner = s > 0 ? 3 - (B & 3) : (B & 3);
+  if (c == aE) return inner + 1;
+  int k = 0;
+  for (int j = 0; j < inner; j++) {
+    const float tj = bound_time(nb + 8 * s * j, o, inv);
+    if (tj < tE || (tj == tE && c < aE)) k++;
+    else break;
+  }
+  return k;
+}
+
 // Walks from voxel (vx,vy,vz) (absolute, inside the grid) at time t, entered
 // through axis ea (-1 none).  Ray coordinates are relative to the absolute
 // voxel (bx0,by0,bz0).
@@ -95,6 +116,7 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
   const float iz = sz ? __fdiv_rn(1.0f, dz) : 0.0f;
   const int px = sx > 0 ? 1 : 0, py = sy > 0 ? 1 : 0, pz = sz > 0 ? 1 : 0;
   const int NBx = V.nx >> 3, NBy = V.ny >> 3, NBz = V.nz >> 3;
+  const int MX = NBx >> 2, MY = NBy >> 2;  // cells of 4x4x4 bricks
   const uint32_t strideY = (uint32_t)NBx, strideZ = (uint32_t)NBx * (uint32_t)NBy;
   // signed index increments of one step along each axis
   const uint32_t dIx = (uint32_t)sx, dIy = (uint32_t)(sy * (int)strideY), dIz = (uint32_t)(sz * (int)strideZ);
@@ -112,14 +134,53 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
     }
     if (p == MESO_EMPTY_BRICK) {
       // ---- coarse: one step per empty brick; nb* = next brick boundary
-      // (relative voxel coordinate) along each axis
+      // (relative voxel coordinate) along each axis.  A cell of 4x4x4 empty
+      // bricks is crossed in one jump (the timed kernel; the statistics
+      // instantiation takes every brick step to count the fetches).
       int nbx = (Bx + px) * 8 - bx0, nby = (By + py) * 8 - by0, nbz = (Bz + pz) * 8 - bz0;
       float tx = sx ? bound_time(nbx, ox, ix) : kInf;
       float ty = sy ? bound_time(nby, oy, iy) : kInf;
       float tz = sz ? bound_time(nbz, oz, iz) : kInf;
       bool out = false;
-      int a;
+      int a = ea;
+      bool empty_cell = !kStats && __ldg(V.macro + (Bx >> 2) + MX * ((By >> 2) + MY * (Bz >> 2))) == 0;
       for (;;) {
+        if (empty_cell) {
+          const float Tx = sx ? bound_time(((Bx >> 2) + px) * 32 - bx0, ox, ix) : kInf;
+          const float Ty = sy ? bound_time(((By >> 2) + py) * 32 - by0, oy, iy) : kInf;
+          const float Tz = sz ? bound_time(((Bz >> 2) + pz) * 32 - bz0, oz, iz) : kInf;
+          const bool my = Ty < Tx;
+          float tE = my ? Ty : Tx;
+          const bool mz = Tz < tE;
+          tE = mz ? Tz : tE;
+          const int aE = mz ? 2 : (my ? 1 : 0);
+          const int kx = cell_steps(0, aE, sx, Bx, nbx, ox, ix, tE);
+          const int ky = cell_steps(1, aE, sy, By, nby, oy, iy, tE);
+          const int kz = cell_steps(2, aE, sz, Bz, nbz, oz, iz, tE);
+          const uint32_t k = (uint32_t)(kx + ky + kz);
+          if (cs + fs + k <= cap) {
+            cs += k;
+            t = tE;
+            a = aE;
+            Bx += sx * kx;
+            By += sy * ky;
+            Bz += sz * kz;
+            idx += dIx * (uint32_t)kx + dIy * (uint32_t)ky + dIz * (uint32_t)kz;
+            nbx += 8 * sx * kx;
+            nby += 8 * sy * ky;
+            nbz += 8 * sz * kz;
+            tx = sx ? bound_time(nbx, ox, ix) : kInf;
+            ty = sy ? bound_time(nby, oy, iy) : kInf;
+            tz = sz ? bound_time(nbz, oz, iz) : kInf;
+            out = ((unsigned)Bx >= (unsigned)NBx) | ((unsigned)By >= (unsigned)NBy) | ((unsigned)Bz >= (unsigned)NBz);
+            if (out || cs + fs > cap) break;
+            p = __ldg(V.ptr + idx);
+            empty_cell = __ldg(V.macro + (Bx >> 2) + MX * ((By >> 2) + MY * (Bz >> 2))) == 0;
+            if (p != MESO_EMPTY_BRICK) break;
+            continue;
+          }
+          empty_cell = false;  // the jump would pass the step cap: take brick steps
+        }
         const bool cy = ty < tx;
         float tm = cy ? ty : tx;
         const bool cz = tz < tm;
@@ -138,6 +199,12 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
         if (kStats) {
           n_fetch++;
           n_brick += p != MESO_EMPTY_BRICK;
+        } else {
+          // entering a new cell: is it empty?
+          const int cnew = a0 ? Bx : (a1 ? By : Bz);
+          const int snew = a0 ? sx : (a1 ? sy : sz);
+          if ((cnew & 3) == (snew > 0 ? 0 : 3))
+            empty_cell = __ldg(V.macro + (Bx >> 2) + MX * ((By >> 2) + MY * (Bz >> 2))) == 0;
         }
         // the next boundary time is computed while the pointer load is in
         // flight; an occupied brick recomputes its times from scratch
@@ -432,6 +499,7 @@ static uint64_t fill_views(const meso_scene* const* scenes, const meso_camera* c
     RayView& V = out[v];
     memset(&V, 0, sizeof(V));
     V.ptr = s->d_ptr;
+    V.macro = s->d_macro;
     V.occ = s->d_occ;
     V.mat = s->d_mat;
     V.nx = s->nx;

@@ -430,6 +430,24 @@ unsigned grid_for(uint64_t warps, int threads = 256) {
 
 }  // namespace
 
+// One warp per macro cell (4x4x4 bricks): any occupied brick -> 1.
+__global__ void macro_kernel(const uint32_t* ptr, int bx, int by, uint8_t* macro, const uint32_t* cells,
+                             uint64_t n) {
+  const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= n) return;
+  const uint32_t m = cells ? cells[w] : (uint32_t)w;
+  const int mx = bx >> 2, my = by >> 2;
+  const int cx = (int)(m % (uint32_t)mx), cy = (int)((m / (uint32_t)mx) % (uint32_t)my), cz = (int)(m / ((uint32_t)mx * my));
+  bool any = false;
+  for (int k = lane; k < 64; k += 32) {
+    const int x = cx * 4 + (k & 3), y = cy * 4 + ((k >> 2) & 3), z = cz * 4 + (k >> 4);
+    any |= ptr[(uint64_t)x + (uint64_t)bx * ((uint64_t)y + (uint64_t)by * z)] != MESO_EMPTY_BRICK;
+  }
+  const bool occupied = __any_sync(0xFFFFFFFFu, any);
+  if (lane == 0) macro[m] = occupied ? 1 : 0;
+}
+
 // ---------------------------------------------------------------- scene API
 
 meso_status scene_alloc(meso_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, uint64_t capacity, meso_scene** out) {
@@ -442,12 +460,14 @@ meso_status scene_alloc(meso_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, uint6
   s->bz = nz / 8;
   s->capacity = capacity;
   const uint64_t nb = n_bricks_of(s);
-  const uint64_t bytes = nb * 4 + capacity * (64 + 1024 + 4) + 16;
+  const uint64_t bytes = nb * 4 + nb / 64 + capacity * (64 + 1024 + 4) + 16;
   if (ctx->budget_bytes && ctx->scene_bytes.load() + bytes > ctx->budget_bytes) {
     delete s;
     return fail(MESO_ERR_OVER_BUDGET, "scene exceeds the HBM budget");
   }
   cudaError_t e = cudaMalloc(&s->d_ptr, nb * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_macro, std::max<uint64_t>(nb / 64, 1));
+  if (e == cudaSuccess) e = cudaMemset(s->d_macro, 0, std::max<uint64_t>(nb / 64, 1));
   if (e == cudaSuccess) e = cudaMalloc(&s->d_occ, std::max<uint64_t>(capacity, 1) * 64);
   if (e == cudaSuccess) e = cudaMalloc(&s->d_mat, std::max<uint64_t>(capacity, 1) * 1024);
   if (e == cudaSuccess) e = cudaMalloc(&s->d_free, std::max<uint64_t>(capacity, 1) * 4);
@@ -467,6 +487,7 @@ meso_status scene_alloc(meso_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, uint6
 void scene_release(meso_ctx* ctx, meso_scene* s) {
   if (!s) return;
   cudaFree(s->d_ptr);
+  cudaFree(s->d_macro);
   cudaFree(s->d_occ);
   cudaFree(s->d_mat);
   cudaFree(s->d_free);
@@ -475,7 +496,18 @@ void scene_release(meso_ctx* ctx, meso_scene* s) {
   delete s;
 }
 
+meso_status rebuild_macro(meso_ctx* ctx, meso_scene* s, const uint32_t* d_cells, uint32_t n, cudaStream_t st) {
+  const uint64_t cells = d_cells ? n : n_macro_of(s);
+  if (cells == 0) return MESO_OK;
+  macro_kernel<<<(unsigned)((cells * 32 + 255) / 256), 256, 0, st>>>(s->d_ptr, s->bx, s->by, s->d_macro, d_cells,
+                                                                     cells);
+  ctx->launches.fetch_add(1);
+  MESO_CUDA_TRY(cudaGetLastError());
+  return MESO_OK;
+}
+
 static meso_status finish_pools(meso_ctx* ctx, meso_scene* s, uint64_t count, cudaStream_t st) {
+  MESO_TRY(rebuild_macro(ctx, s, nullptr, 0, st));
   int32_t init[4] = {(int32_t)count, 0, 0, 0};
   MESO_CUDA_TRY(cudaMemcpyAsync(s->d_alloc, init, 16, cudaMemcpyHostToDevice, st));
   MESO_CUDA_TRY(cudaStreamSynchronize(st));
@@ -683,15 +715,29 @@ meso_status edit_spheres(meso_ctx* ctx, meso_scene* s, const meso_sphere_edit* h
   if (h_dirty) std::copy(chunks.begin(), chunks.begin() + std::min<size_t>(chunks.size(), dirty_cap), h_dirty);
   if (bricks.empty()) return chunks.size() > dirty_cap && h_dirty ? fail(MESO_ERR_OVERFLOW, "edit: dirty list overflow") : MESO_OK;
   const size_t nb = bricks.size();
-  const size_t bytes = n * sizeof(meso_sphere_edit) + nb * 4 + nb * 1024 + nb + 64;
+  // macro cells holding the touched bricks (sorted unique)
+  std::vector<uint32_t> cells;
+  cells.reserve(nb);
+  for (uint32_t b : bricks) {
+    const uint32_t x = b % (uint32_t)s->bx, y = (b / (uint32_t)s->bx) % (uint32_t)s->by,
+                   z = b / ((uint32_t)s->bx * (uint32_t)s->by);
+    cells.push_back((x >> 2) + (uint32_t)(s->bx >> 2) * ((y >> 2) + (uint32_t)(s->by >> 2) * (z >> 2)));
+  }
+  std::sort(cells.begin(), cells.end());
+  cells.erase(std::unique(cells.begin(), cells.end()), cells.end());
+  const size_t nc = cells.size();
+  const size_t bytes = n * sizeof(meso_sphere_edit) + nb * 4 + nb * 1024 + nb + 64 + nc * 4 + 16;
   uint8_t* d = nullptr;
   MESO_CUDA_TRY(cudaMallocAsync(&d, bytes, st));
   meso_sphere_edit* d_sp = reinterpret_cast<meso_sphere_edit*>(d);
   uint32_t* d_b = reinterpret_cast<uint32_t*>(d + n * sizeof(meso_sphere_edit));
   uint16_t* d_temp = reinterpret_cast<uint16_t*>(d + ((n * sizeof(meso_sphere_edit) + nb * 4 + 15) & ~size_t(15)));
   uint8_t* d_state = reinterpret_cast<uint8_t*>(d_temp) + nb * 1024;
+  uint32_t* d_cells = reinterpret_cast<uint32_t*>(d + ((n * sizeof(meso_sphere_edit) + nb * 4 + 15) & ~size_t(15)) +
+                                                  ((nb * 1024 + nb + 15) & ~size_t(15)));
   MESO_CUDA_TRY(cudaMemcpyAsync(d_sp, h_sp, n * sizeof(meso_sphere_edit), cudaMemcpyHostToDevice, st));
   MESO_CUDA_TRY(cudaMemcpyAsync(d_b, bricks.data(), nb * 4, cudaMemcpyHostToDevice, st));
+  MESO_CUDA_TRY(cudaMemcpyAsync(d_cells, cells.data(), nc * 4, cudaMemcpyHostToDevice, st));
   EditParams P;
   P.spheres = d_sp;
   P.n_spheres = n;
@@ -713,6 +759,7 @@ meso_status edit_spheres(meso_ctx* ctx, meso_scene* s, const meso_sphere_edit* h
   edit_alloc_kernel<<<blocks, 256, 0, st>>>(P);
   edit_fix_kernel<<<1, 1, 0, st>>>(P.alloc, P.capacity);
   ctx->launches.fetch_add(3);
+  MESO_TRY(rebuild_macro(ctx, s, d_cells, (uint32_t)nc, st));
   MESO_CUDA_TRY(cudaFreeAsync(d, st));
   MESO_CUDA_TRY(cudaGetLastError());
   if (h_dirty && chunks.size() > dirty_cap) return fail(MESO_ERR_OVERFLOW, "edit: dirty list overflow");

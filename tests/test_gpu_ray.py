@@ -4,6 +4,8 @@ Hit voxel, face, material, shadow flag and step counts are compared bit for
 bit; the hit distance t within 1e-6 relative (it is in fact bit-identical:
 both sides evaluate the same sequence of correctly rounded FP32 operations).
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -127,6 +129,48 @@ def test_raymarch_host_pinned_direct(ctx, small, height):
     got = buf.view(meso.HIT_DTYPE, w * height).copy()
     buf.free()
     assert_hits_equal(got, oracle.raymarch(bm, ocam))
+
+
+@pytest.fixture(scope="module")
+def sparse(ctx):
+    # 256 x 192 x 128 voxels (x, y, z), a few boxes: most 32^3 cells empty
+    rng = np.random.default_rng(3)
+    g = np.zeros((128, 192, 256), np.uint16)  # [z][y][x]
+    for _ in range(30):
+        c = rng.integers(0, (128, 192, 256))
+        r = rng.integers(1, 7, 3)
+        g[max(c[0] - r[0], 0):c[0] + r[0], max(c[1] - r[1], 0):c[1] + r[1], max(c[2] - r[2], 0):c[2] + r[2]] = \
+            rng.integers(1, 200)
+    return ctx.scene_from_dense(g, spare_bricks=4096), oracle.HostBrickMap.from_dense(g)
+
+
+def test_empty_cell_jumps_match_oracle(ctx, sparse):
+    # the timed kernel crosses empty 4x4x4-brick cells in one jump and adds
+    # their brick steps arithmetically; hits, t and both step counts must be
+    # those of the brick-by-brick walk, including exact ties (the centre ray
+    # of the first camera runs along (1,1,1) through cell corners)
+    scene, bm = sparse
+    poses = [((-64.0, -64.0, -64.0), (64.0, 64.0, 64.0)), ((-32.0, 96.0, 300.0), (96.0, 96.0, 0.0)),
+             ((0.0, 0.0, 0.0), (255.0, 191.0, 127.0)), ((128.0, -10.0, 64.0), (128.0, 300.0, 64.0)),
+             ((300.0, 250.0, 200.0), (10.0, 20.0, 5.0)), ((32.0, 32.0, 32.0), (33.0, 200.0, 100.0))]
+    rng = np.random.default_rng(11)
+    for _ in range(10):
+        o = rng.uniform(-150, 400, 3)
+        poses.append((tuple(o), tuple(rng.uniform(0, (256, 192, 128)))))
+    for o, tg in poses:
+        cam = meso.camera(o, tg, 48, 40)
+        assert_hits_equal(ctx.raymarch(scene, cam), oracle.raymarch(bm, oracle.camera(o, tg, 48, 40)))
+
+
+def test_empty_cell_map_follows_edits(ctx, sparse):
+    # carve whole cells empty and fill empty ones, then render
+    scene, bm = sparse
+    sp = [((80, 80, 60), 40, 0), ((200, 40, 100), 12, 7), ((20, 150, 20), 9, 300), ((128, 96, 64), 30, 0)]
+    scene.edit([meso.SphereEdit((ctypes.c_int32 * 3)(*c), r, m, 0) for c, r, m in sp])
+    bm.edit([oracle.Sphere((ctypes.c_int32 * 3)(*c), r, m, 0) for c, r, m in sp])
+    for o, tg in [((-64.0, -64.0, -64.0), (128.0, 96.0, 64.0)), ((300.0, 250.0, 200.0), (80.0, 80.0, 60.0))]:
+        cam = meso.camera(o, tg, 64, 48)
+        assert_hits_equal(ctx.raymarch(scene, cam), oracle.raymarch(bm, oracle.camera(o, tg, 64, 48)))
 
 
 def test_matches_golden_fixture(ctx, small):
