@@ -30,6 +30,7 @@ struct RayView {
   float o[3];
   float fwd[3], right[3], up[3];
   float tan_half;
+  float aspect;  // width / height, correctly rounded
   uint32_t width, height;
   uint32_t tiles_x;
   uint32_t tile_start;
@@ -53,6 +54,7 @@ struct RayParams {
   uint32_t total_tiles;
   uint32_t tile_w, tile_h;
   float light[3];
+  float inv_light[3];  // 1 / light per axis, correctly rounded (0 for a zero component)
   uint32_t shadow;
   meso_hit* hits;
   uint64_t* stats;
@@ -95,7 +97,7 @@ __device__ __forceinline__ int cell_steps(int c, int aE, int s, int B, int nb, f
 
 // Walks from voxel (vx,vy,vz) (absolute, inside the grid) at time t, entered
 // through axis ea (-1 none).  Ray coordinates are relative to the absolute
-// voxel (bx0,by0,bz0).
+// voxel (bx0,by0,bz0); ix, iy, iz are 1/d per axis (0 where d is 0).
 //
 // The walk is the same sequence of float operations as a step-by-step
 // recomputation, organised for issue efficiency: a boundary time is only
@@ -105,15 +107,12 @@ __device__ __forceinline__ int cell_steps(int c, int aE, int s, int B, int nb, f
 // word of the current z layer stays in a register.
 template <bool kStats>
 __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int bz0, float ox, float oy, float oz,
-                                         float dx, float dy, float dz, int vx, int vy, int vz, float t, int ea,
-                                         Trav& r) {
+                                         float dx, float dy, float dz, float ix, float iy, float iz, int vx, int vy,
+                                         int vz, float t, int ea, Trav& r) {
   uint32_t n_fetch = 0, n_brick = 0;
   const int sx = dx > 0.0f ? 1 : (dx < 0.0f ? -1 : 0);
   const int sy = dy > 0.0f ? 1 : (dy < 0.0f ? -1 : 0);
   const int sz = dz > 0.0f ? 1 : (dz < 0.0f ? -1 : 0);
-  const float ix = sx ? __fdiv_rn(1.0f, dx) : 0.0f;
-  const float iy = sy ? __fdiv_rn(1.0f, dy) : 0.0f;
-  const float iz = sz ? __fdiv_rn(1.0f, dz) : 0.0f;
   const int px = sx > 0 ? 1 : 0, py = sy > 0 ? 1 : 0, pz = sz > 0 ? 1 : 0;
   const int NBx = V.nx >> 3, NBy = V.ny >> 3, NBz = V.nz >> 3;
   const int MX = NBx >> 2, MY = NBy >> 2;  // cells of 4x4x4 bricks
@@ -144,6 +143,7 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
       bool out = false;
       int a = ea;
       bool empty_cell = !kStats && __ldg(V.macro + (Bx >> 2) + MX * ((By >> 2) + MY * (Bz >> 2))) == 0;
+      bool stale = false;
       for (;;) {
         if (empty_cell) {
           const float Tx = sx ? bound_time(((Bx >> 2) + px) * 32 - bx0, ox, ix) : kInf;
@@ -169,9 +169,7 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
             nbx += 8 * sx * kx;
             nby += 8 * sy * ky;
             nbz += 8 * sz * kz;
-            tx = sx ? bound_time(nbx, ox, ix) : kInf;
-            ty = sy ? bound_time(nby, oy, iy) : kInf;
-            tz = sz ? bound_time(nbz, oz, iz) : kInf;
+            stale = true;  // brick boundary times: recomputed if a brick step follows
             out = ((unsigned)Bx >= (unsigned)NBx) | ((unsigned)By >= (unsigned)NBy) | ((unsigned)Bz >= (unsigned)NBz);
             if (out || cs + fs > cap) break;
             p = __ldg(V.ptr + idx);
@@ -180,6 +178,12 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
             continue;
           }
           empty_cell = false;  // the jump would pass the step cap: take brick steps
+        }
+        if (stale) {
+          tx = sx ? bound_time(nbx, ox, ix) : kInf;
+          ty = sy ? bound_time(nby, oy, iy) : kInf;
+          tz = sz ? bound_time(nbz, oz, iz) : kInf;
+          stale = false;
         }
         const bool cy = ty < tx;
         float tm = cy ? ty : tx;
@@ -303,7 +307,7 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
 __device__ __forceinline__ void camera_ray(const RayView& V, uint32_t px, uint32_t py, float& dx, float& dy,
                                            float& dz) {
   const float fw = __uint2float_rn(V.width), fh = __uint2float_rn(V.height);
-  const float aspect = __fdiv_rn(fw, fh);
+  const float aspect = V.aspect;
   float sxv = __fdiv_rn(__uint2float_rn(2u * px + 1u), fw);
   sxv = __fsub_rn(sxv, 1.0f);
   sxv = __fmul_rn(sxv, V.tan_half);
@@ -340,6 +344,9 @@ __device__ __forceinline__ void trace_pixel(const RayView& V, uint32_t px, uint3
   const int sx = dx > 0.0f ? 1 : (dx < 0.0f ? -1 : 0);
   const int sy = dy > 0.0f ? 1 : (dy < 0.0f ? -1 : 0);
   const int sz = dz > 0.0f ? 1 : (dz < 0.0f ? -1 : 0);
+  const float ix = sx ? __fdiv_rn(1.0f, dx) : 0.0f;
+  const float iy = sy ? __fdiv_rn(1.0f, dy) : 0.0f;
+  const float iz = sz ? __fdiv_rn(1.0f, dz) : 0.0f;
   // slab test against [-base, N - base)
   float tnear = -kInf, tfar = kInf;
   int ea = -1;
@@ -348,7 +355,7 @@ __device__ __forceinline__ void trace_pixel(const RayView& V, uint32_t px, uint3
     if (!sx) {
       if (ox < lo || ox >= hi) return;
     } else {
-      const float inv = __fdiv_rn(1.0f, dx);
+      const float inv = ix;
       const float t1 = __fmul_rn(__fsub_rn(lo, ox), inv), t2 = __fmul_rn(__fsub_rn(hi, ox), inv);
       const float tn = sx > 0 ? t1 : t2, tf = sx > 0 ? t2 : t1;
       if (tn > tnear) { tnear = tn; ea = 0; }
@@ -360,7 +367,7 @@ __device__ __forceinline__ void trace_pixel(const RayView& V, uint32_t px, uint3
     if (!sy) {
       if (oy < lo || oy >= hi) return;
     } else {
-      const float inv = __fdiv_rn(1.0f, dy);
+      const float inv = iy;
       const float t1 = __fmul_rn(__fsub_rn(lo, oy), inv), t2 = __fmul_rn(__fsub_rn(hi, oy), inv);
       const float tn = sy > 0 ? t1 : t2, tf = sy > 0 ? t2 : t1;
       if (tn > tnear) { tnear = tn; ea = 1; }
@@ -372,7 +379,7 @@ __device__ __forceinline__ void trace_pixel(const RayView& V, uint32_t px, uint3
     if (!sz) {
       if (oz < lo || oz >= hi) return;
     } else {
-      const float inv = __fdiv_rn(1.0f, dz);
+      const float inv = iz;
       const float t1 = __fmul_rn(__fsub_rn(lo, oz), inv), t2 = __fmul_rn(__fsub_rn(hi, oz), inv);
       const float tn = sz > 0 ? t1 : t2, tf = sz > 0 ? t2 : t1;
       if (tn > tnear) { tnear = tn; ea = 2; }
@@ -398,7 +405,7 @@ __device__ __forceinline__ void trace_pixel(const RayView& V, uint32_t px, uint3
     vz = clampi((int)floorf(oz) + bz0, 0, V.nz - 1);
   }
   Trav r;
-  traverse<kStats>(V, bx0, by0, bz0, ox, oy, oz, dx, dy, dz, vx, vy, vz, t0, ea, r);
+  traverse<kStats>(V, bx0, by0, bz0, ox, oy, oz, dx, dy, dz, ix, iy, iz, vx, vy, vz, t0, ea, r);
   h.steps = r.fine | (r.coarse << 16);
   if (kStats) {
     st[0] += r.fetches;
@@ -428,7 +435,8 @@ __device__ __forceinline__ void trace_pixel(const RayView& V, uint32_t px, uint3
     return;
   }
   Trav sr;
-  traverse<kStats>(V, Sx, Sy, Sz, 0.5f, 0.5f, 0.5f, P.light[0], P.light[1], P.light[2], Sx, Sy, Sz, 0.0f, -1, sr);
+  traverse<kStats>(V, Sx, Sy, Sz, 0.5f, 0.5f, 0.5f, P.light[0], P.light[1], P.light[2], P.inv_light[0],
+                   P.inv_light[1], P.inv_light[2], Sx, Sy, Sz, 0.0f, -1, sr);
   if (kStats) {
     st[0] += sr.fetches;
     st[1] += sr.bricks;
@@ -513,6 +521,7 @@ static uint64_t fill_views(const meso_scene* const* scenes, const meso_camera* c
       V.up[a] = c.up[a];
     }
     V.tan_half = c.tan_half_fov_y;
+    V.aspect = (float)c.width / (float)c.height;  // IEEE conversions and division, as on the device
     V.width = c.width;
     V.height = c.height;
     V.tiles_x = (c.width + tw - 1) / tw;
@@ -547,7 +556,10 @@ meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, cons
   P.tile_h = th;
   P.shadow = (flags & MESO_RAY_SHADOW) ? 1u : 0u;
   if (light)
-    for (int a = 0; a < 3; a++) P.light[a] = light[a];
+    for (int a = 0; a < 3; a++) {
+      P.light[a] = light[a];
+      P.inv_light[a] = light[a] != 0.0f ? 1.0f / light[a] : 0.0f;  // IEEE division, as __fdiv_rn
+    }
   P.hits = d_hits;
   P.stats = d_stats;
   static InlineViews empty_views;  // zero-initialised
@@ -666,7 +678,10 @@ extern "C" meso_status meso_raymarch_noalloc(meso_ctx* ctx, const meso_scene* co
   P.tile_h = th;
   P.shadow = (flags & MESO_RAY_SHADOW) ? 1u : 0u;
   if (light)
-    for (int a = 0; a < 3; a++) P.light[a] = light[a];
+    for (int a = 0; a < 3; a++) {
+      P.light[a] = light[a];
+      P.inv_light[a] = light[a] != 0.0f ? 1.0f / light[a] : 0.0f;  // IEEE division, as __fdiv_rn
+    }
   P.hits = d_hits;
   const cudaStream_t st = pick_stream(ctx, stream);
   // pageable source: the copy is staged before cudaMemcpyAsync returns
