@@ -280,6 +280,68 @@ def cpu_mesh_baseline(m, n_single=512):
             "parity_bit_exact": parity}
 
 
+def bench_downstream(ctx, meso, m, steps):
+    """The steps either side of the hot paths: device scene build, quad ->
+    vertex expansion and the erosion pyramid on the batched-meshing data."""
+    import ctypes
+    L = meso._lib
+    hbm = peaks()[0]
+    res = {}
+    # device scene build of the 1024^3 terrain (pointer grid + pools written)
+    t0 = time.perf_counter()
+    sc = ctx.scene_from_terrain(meso.terrain_preset("scene1024"))
+    build_s = time.perf_counter() - t0
+    info = sc.info()
+    written = info.n_bricks * (64 + 1024) + (1024 // 8) ** 3 * 4
+    res["scene_build"] = {"workload": "1024^3 terrain (6-octave fBm heightfield, caves), device generator + scan",
+                          "ms": round(build_s * 1e3, 2), "bricks": int(info.n_bricks),
+                          "gb_s_written": round(written / build_s / 1e9, 1)}
+    sc.destroy()
+    # quad -> vertex expansion of the batched mesh output (8 B in, 64 B out per quad)
+    nq = m["quads"]
+    origins = ctx.to_device(np.stack([np.arange(MESH_CHUNKS), np.zeros(MESH_CHUNKS), np.zeros(MESH_CHUNKS)], 1)
+                            .astype(np.int32))
+    verts = ctx.alloc(nq * 64)
+    flush = ctx.alloc(L2_FLUSH_BYTES)
+
+    def timed(fn):
+        fn()
+        ctx.sync()
+        tot = 0.0
+        for _ in range(steps):
+            flush.zero()
+            a, b = ctx.event(), ctx.event()
+            ctx.record(a)
+            fn()
+            ctx.record(b)
+            ctx.sync()
+            tot += ctx.elapsed_ms(a, b)
+        return tot / steps
+
+    ms = timed(lambda: meso._check(L.meso_quads_to_vertices(ctx.handle, m["qbuf"].ptr, nq, origins.ptr,
+                                                            MESH_CHUNKS, verts.ptr, None)))
+    ach = nq * 72 / (ms * 1e6)
+    res["quads_to_vertices"] = {"quads": nq, "ms": round(ms, 4), "roofline": {
+        "bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4),
+        "algorithmic_bytes_per_launch": nq * 72}}
+    verts.free()
+    # erosion pyramid (4 mips) of the 4096 standalone chunks: 64 KiB in, 4 x 4 KiB out per chunk
+    out = ctx.alloc(MESH_CHUNKS * 4 * 4096)
+    src = meso.MeshSource()
+    src.kind = meso.SRC_CHUNKS_U16
+    src.d_data = m["data"].ptr
+    ms = timed(lambda: meso._check(L.meso_erode_mips(ctx.handle, ctypes.byref(src), None, MESH_CHUNKS, 4, out.ptr,
+                                                     None)))
+    algo = MESH_CHUNKS * (65536 + 4 * 4096)
+    ach = algo / (ms * 1e6)
+    res["erode_mips"] = {"workload": f"{MESH_CHUNKS} chunks of 32^3 uint16, 4 mips", "ms": round(ms, 4),
+                         "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+                                      "frac": round(ach / hbm, 4), "algorithmic_bytes_per_launch": algo}}
+    out.free()
+    flush.free()
+    return res
+
+
 def poisson_arrivals(rate, seconds, seed):
     rng = np.random.default_rng(seed)
     t, out = 0.0, []
@@ -547,6 +609,7 @@ def run_ours(args, world, rank, local, dist):
         }
         if not args.skip_cpu:
             line["mesh"]["cpu_baseline"] = cpu_mesh_baseline(m)
+        line["downstream"] = bench_downstream(ctx, meso, m, args.steps)
     if rank == 0 and not args.skip_serve:
         line["served"] = bench_serve_render(ctx, meso, args.serve_seconds)
         line["served_edit"] = bench_serve_edit(ctx, meso, args.serve_seconds)

@@ -374,7 +374,8 @@ typedef struct meso_vertex {
  * triples, device).  The step after meshing for a raster consumer; replaces
  * the reference's per-block FGPUBlock instance stream
  * (Runtimes/Voxel/Block/Block.h:21-65) and the corner placement of its
- * imposter vertex shader (Samples/SimpleVoxel.cpp:171-189). */
+ * imposter vertex shader (Samples/SimpleVoxel.cpp:171-189).  d_out must be
+ * 16-byte aligned. */
 meso_status meso_quads_to_vertices(meso_ctx* ctx, const uint64_t* d_quads, uint64_t n_quads,
                                    const int32_t* d_chunk_origins, uint32_t n_chunks, meso_vertex* d_out,
                                    void* stream);

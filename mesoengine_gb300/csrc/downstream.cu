@@ -18,9 +18,12 @@ constexpr uint32_t kFull = 0xFFFFFFFFu;
 
 // ------------------------------------------------------------ vertices
 // Plane axes per face direction: X faces u=y v=z; Y faces u=x v=z; Z faces u=x v=y.
+// One thread per vertex (4 per quad), so a warp stores 512 contiguous bytes.
 __global__ void quads_to_vertices_kernel(const uint64_t* quads, uint64_t n, const int32_t* origins,
                                          uint32_t n_chunks, meso_vertex* out, uint32_t* err) {
-  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  const uint64_t vi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  const uint64_t i = vi >> 2;
+  const int k = (int)(vi & 3u);
   if (i >= n) return;
   const uint64_t q = quads[i];
   const uint32_t chunk = (uint32_t)(q >> 44);
@@ -33,7 +36,7 @@ __global__ void quads_to_vertices_kernel(const uint64_t* quads, uint64_t n, cons
     ox = origins[3 * chunk] * 32;
     oy = origins[3 * chunk + 1] * 32;
     oz = origins[3 * chunk + 2] * 32;
-  } else {
+  } else if (k == 0) {
     atomicOr(err, ERR_BAD_INPUT);
   }
   const int a = dir >> 1;
@@ -47,24 +50,20 @@ __global__ void quads_to_vertices_kernel(const uint64_t* quads, uint64_t n, cons
   // u x v points along +a for X and Z faces and along -a for Y faces; keep
   // the corner order when that matches the face normal, reverse it otherwise
   const bool natural = (a == 1) ? !plus : plus;
-  meso_vertex* dst = out + 4 * i;
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    // corners (u0,v0), (u0+w,v0), (u0+w,v0+h), (u0,v0+h)
-    const int c = natural ? k : (4 - k) & 3;
-    const int cu = (c == 1 || c == 2) ? u0 + w : u0;
-    const int cv = c >= 2 ? v0 + h : v0;
-    int x, y, z;
-    if (a == 0) { x = plane; y = cu; z = cv; }
-    else if (a == 1) { y = plane; x = cu; z = cv; }
-    else { z = plane; x = cu; y = cv; }
-    meso_vertex vtx;
-    vtx.x = (float)(ox + x);
-    vtx.y = (float)(oy + y);
-    vtx.z = (float)(oz + z);
-    vtx.attr = mat | (uint32_t)dir << 16 | (uint32_t)k << 19;
-    dst[k] = vtx;
-  }
+  // corners (u0,v0), (u0+w,v0), (u0+w,v0+h), (u0,v0+h)
+  const int c = natural ? k : (4 - k) & 3;
+  const int cu = (c == 1 || c == 2) ? u0 + w : u0;
+  const int cv = c >= 2 ? v0 + h : v0;
+  int x, y, z;
+  if (a == 0) { x = plane; y = cu; z = cv; }
+  else if (a == 1) { y = plane; x = cu; z = cv; }
+  else { z = plane; x = cu; y = cv; }
+  float4 vtx;
+  vtx.x = (float)(ox + x);
+  vtx.y = (float)(oy + y);
+  vtx.z = (float)(oz + z);
+  vtx.w = __uint_as_float(mat | (uint32_t)dir << 16 | (uint32_t)k << 19);
+  reinterpret_cast<float4*>(out)[vi] = vtx;
 }
 
 // ------------------------------------------------------------ erosion
@@ -135,14 +134,47 @@ __global__ void __launch_bounds__(256) erode_kernel(const ErodeParams p) {
     for (uint32_t i = threadIdx.x; i < p.depth * 1024; i += blockDim.x) out[i] = 0;
     return;
   }
-  for (int row = warp; row < 1024; row += 8) {
-    const int z = row >> 5, y = row & 31;
-    const uint32_t w = __ballot_sync(kFull, chunk_voxel(p, c, cx, cy, cz, lane, y, z));
-    if (lane == 0) {
-      mip0[row] = w;
-      cur[row] = w;
-      out[row] = w;
+  if (p.kind == MESO_SRC_CHUNKS_U16 || p.kind == MESO_SRC_CHUNKS_U8) {
+    // contiguous chunk: 16-byte loads, each giving the occupancy bits of 8
+    // (uint16) or 16 (uint8) consecutive voxels of a row, written to the
+    // row word in shared memory as a byte or a half word (bit x = voxel x)
+    const uint32_t idx = p.coords ? (uint32_t)p.coords[c] : c;
+    if (p.kind == MESO_SRC_CHUNKS_U16) {
+      const uint4* src = reinterpret_cast<const uint4*>(p.data + (size_t)idx * 65536u);
+      uint8_t* dst = reinterpret_cast<uint8_t*>(mip0);
+      for (int i = threadIdx.x; i < 4096; i += blockDim.x) {
+        const uint4 v = __ldg(src + i);
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+        uint32_t b = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) b |= ((w[k] & 0xFFFFu) != 0 ? 1u : 0u) << (2 * k) | ((w[k] >> 16) != 0 ? 2u : 0u) << (2 * k);
+        dst[i] = (uint8_t)b;
+      }
+    } else {
+      const uint4* src = reinterpret_cast<const uint4*>(p.data + (size_t)idx * 32768u);
+      uint16_t* dst = reinterpret_cast<uint16_t*>(mip0);
+      for (int i = threadIdx.x; i < 2048; i += blockDim.x) {
+        const uint4 v = __ldg(src + i);
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+        uint32_t b = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+#pragma unroll
+          for (int j = 0; j < 4; j++) b |= (((w[k] >> (8 * j)) & 0xFFu) != 0 ? 1u : 0u) << (4 * k + j);
+        dst[i] = (uint16_t)b;
+      }
     }
+  } else {
+    for (int row = warp; row < 1024; row += 8) {
+      const int z = row >> 5, y = row & 31;
+      const uint32_t w = __ballot_sync(kFull, chunk_voxel(p, c, cx, cy, cz, lane, y, z));
+      if (lane == 0) mip0[row] = w;
+    }
+  }
+  __syncthreads();
+  for (int row = threadIdx.x; row < 1024; row += blockDim.x) {
+    cur[row] = mip0[row];
+    out[row] = mip0[row];
   }
   __syncthreads();
   for (uint32_t d = 1; d < p.depth; d++) {
@@ -183,8 +215,10 @@ meso_status meso_quads_to_vertices(meso_ctx* ctx, const uint64_t* d_quads, uint6
   if (!ctx || (n && (!d_quads || !d_origins || !d_out)))
     return fail(MESO_ERR_INVALID_ARG, "quads_to_vertices: null argument");
   if (n == 0) return MESO_OK;
+  if (reinterpret_cast<uintptr_t>(d_out) & 15u)
+    return fail(MESO_ERR_INVALID_ARG, "quads_to_vertices: output must be 16-byte aligned");
   const cudaStream_t st = pick_stream(ctx, stream);
-  const uint64_t blocks = (n + 255) / 256;
+  const uint64_t blocks = (4 * n + 255) / 256;
   if (blocks > 0x7FFFFFFFull) return fail(MESO_ERR_INVALID_ARG, "quads_to_vertices: too many quads");
   quads_to_vertices_kernel<<<(unsigned)blocks, 256, 0, st>>>(d_quads, n, d_origins, n_chunks, d_out,
                                                              ctx->d_scratch + 1);
@@ -221,6 +255,8 @@ meso_status meso_erode_mips(meso_ctx* ctx, const meso_mesh_source* src, const in
       return fail(MESO_ERR_INVALID_ARG, "erode_mips: grid needs coords and dims multiple of 32");
     if (!grid && d_coords && src->nx <= 0)
       return fail(MESO_ERR_INVALID_ARG, "erode_mips: an index list needs nx = chunks in the array");
+    if (!grid && (reinterpret_cast<uintptr_t>(src->d_data) & 15u))
+      return fail(MESO_ERR_INVALID_ARG, "erode_mips: chunk array must be 16-byte aligned");
     p.data = static_cast<const uint8_t*>(src->d_data);
     p.nx = src->nx;
     p.ny = src->ny;

@@ -33,6 +33,19 @@ def test_erode_mips_chunk_array_matches_reference_loop(ctx):
     assert _bits_to_dense(got[-1])[3].sum() > 0
 
 
+def test_erode_mips_u8_chunks_with_index_list(ctx):
+    # uint8 chunk arrays take the 16-byte load path too; an index list picks
+    # chunks out of order and repeats one
+    rng = np.random.default_rng(5)
+    chunks = ((rng.random((6, 32, 32, 32)) < 0.8) * rng.integers(1, 255, (6, 32, 32, 32))).astype(np.uint8)
+    chunks[2] = 0
+    chunks[3, 1:31, 1:31, 1:31] = 9
+    idx = np.array([[3], [0], [5], [3], [2]], dtype=np.int32)
+    got = ctx.erode_mips(meso.SRC_CHUNKS_U8, ctx.to_device(chunks), coords=idx, depth=4)
+    for i, c in enumerate(idx[:, 0]):
+        assert np.array_equal(_bits_to_dense(got[i]), oracle.erode_mips(chunks[c], 4)), i
+
+
 def test_erode_mips_grid_and_brickmap(ctx):
     g = ctx.generate_dense_u8(64, 64, 64, seed=3)
     grid = g.download(np.uint8).reshape(64, 64, 64)
