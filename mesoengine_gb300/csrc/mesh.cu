@@ -631,14 +631,8 @@ __global__ void __launch_bounds__(kThreads, 2)
           const int sh_u = dir < 2 ? 5 : 0;
           const int sh_v = dir < 4 ? 10 : 5;
           const uint64_t dir_bits = chunk_bits | (uint64_t)dir << 41;
-          for (uint32_t k2 = 0; k2 < G; k2 += 32) {
-            const uint32_t j = k2 + (uint32_t)lane;
-            int l = 0;
-#pragma unroll
-            for (int step = 16; step >= 1; step >>= 1) {
-              const uint32_t oc = __shfl_sync(kFull, ex, l + step);
-              if (oc <= j) l += step;
-            }
+          // two rounds (64 bits) per pass, so their shuffle chains interleave
+          auto emit = [&](uint32_t j, int l) {
             const uint32_t r = j - __shfl_sync(kFull, ex, l);
             const uint32_t pk = __shfl_sync(kFull, packed, l);
             const uint32_t x0 = __shfl_sync(kFull, w0, l), x1 = __shfl_sync(kFull, w1, l);
@@ -656,6 +650,19 @@ __global__ void __launch_bounds__(kThreads, 2)
               const unsigned long long idx = run + j;
               if (idx < p.cap) p.quads[idx] = dir_bits | (uint64_t)lin << 26 | mat;
             }
+          };
+          for (uint32_t k2 = 0; k2 < G; k2 += 64) {
+            const uint32_t ja = k2 + (uint32_t)lane, jb = ja + 32u;
+            int la = 0, lb = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+              const uint32_t oa = __shfl_sync(kFull, ex, la + step);
+              const uint32_t ob = __shfl_sync(kFull, ex, lb + step);
+              if (oa <= ja) la += step;
+              if (ob <= jb) lb += step;
+            }
+            emit(ja, la);
+            if (k2 + 32u < G) emit(jb, lb);
           }
           run += G;
         }
