@@ -76,6 +76,13 @@ meso_status meso_sync(meso_ctx* ctx, void* stream);
 /* Number of mesher/raymarch/scene kernels this context has launched. */
 uint64_t meso_kernel_launches(const meso_ctx* ctx);
 int meso_sm_count(const meso_ctx* ctx);
+/* Diagnostic of the failure path (no counterpart in the reference): runs a
+ * kernel whose bounded device wait cannot succeed (an mbarrier nothing
+ * arrives on, waited for with the helper that guards every TMA copy of the
+ * mesher).  The wait gives up after limit_us (1 .. 1,000,000), the kernel
+ * flags the timeout and exits, and the call returns MESO_ERR_TIMEOUT; the
+ * context stays usable. */
+meso_status meso_selftest_bounded_wait(meso_ctx* ctx, uint32_t limit_us);
 
 /* Device memory, streams and events for callers without another CUDA host
  * library (tests, the Python binding). */

@@ -193,6 +193,7 @@ _SIGNATURES = {
     "meso_capture_end": [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)],
     "meso_graph_launch": [ctypes.c_void_p, ctypes.c_void_p],
     "meso_graph_destroy": [ctypes.c_void_p],
+    "meso_selftest_bounded_wait": [ctypes.c_void_p, ctypes.c_uint32],
     "meso_raymarch_noalloc": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Camera),
                               ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p],
 }
@@ -593,6 +594,11 @@ class Context:
         _check(_lib.meso_erode_mips(self.handle, ctypes.byref(src), cb.ptr if cb else None, n, depth, out.ptr, None))
         self.sync()
         return out.download(np.uint32, n * depth * 1024).reshape(n, depth, 32, 32)
+
+    def selftest_bounded_wait(self, limit_us: int) -> None:
+        """Runs a device wait that must give up after limit_us; raises
+        MesoError(MESO_ERR_TIMEOUT) when the failure path works."""
+        _check(_lib.meso_selftest_bounded_wait(self.handle, limit_us))
 
     def autotune(self, path: str | None = None) -> None:
         _check(_lib.meso_autotune(self.handle, path.encode() if path else None))

@@ -63,6 +63,21 @@ static void load_tuning(const char* path, Tuning& t) {
 
 using namespace meso;
 
+namespace {
+// An mbarrier that nothing arrives on: its phase 0 never completes, so the
+// bounded wait must give up; the kernel flags it as every copy wait does.
+__global__ void bounded_wait_probe_kernel(uint64_t limit_ns, uint32_t* err) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    meso::dev::mbar_init(&bar, 1);
+    meso::dev::fence_proxy_async_smem();
+  }
+  __syncthreads();
+  const bool ok = meso::dev::mbar_wait_bounded(&bar, 0, limit_ns);
+  if (!ok && threadIdx.x == 0) atomicOr(err, meso::ERR_TIMEOUT);
+}
+}  // namespace
+
 extern "C" {
 
 const char* meso_last_error_string(void) { return g_err.c_str(); }
@@ -151,6 +166,16 @@ meso_status meso_sync(meso_ctx* ctx, void* stream) {
     if (err & ERR_BAD_INPUT) return fail(MESO_ERR_INVALID_ARG, "chunk coordinate outside the source");
   }
   return MESO_OK;
+}
+
+
+meso_status meso_selftest_bounded_wait(meso_ctx* ctx, uint32_t limit_us) {
+  if (!ctx || limit_us == 0 || limit_us > 1000000)
+    return fail(MESO_ERR_INVALID_ARG, "selftest_bounded_wait: limit must be 1..1000000 us");
+  bounded_wait_probe_kernel<<<1, 32, 0, ctx->stream>>>((uint64_t)limit_us * 1000u, ctx->d_scratch + 1);
+  ctx->launches.fetch_add(1);
+  MESO_CUDA_TRY(cudaGetLastError());
+  return meso_sync(ctx, nullptr);
 }
 
 uint64_t meso_kernel_launches(const meso_ctx* ctx) { return ctx ? ctx->launches.load() : 0; }
