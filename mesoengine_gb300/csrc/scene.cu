@@ -541,10 +541,17 @@ meso_status scene_create_terrain(meso_ctx* ctx, const meso_terrain* t, uint64_t 
   float* d_hmax = nullptr;
   uint8_t* d_flags = nullptr;
   uint32_t* d_ptr_tmp = nullptr;
-  MESO_CUDA_TRY(cudaMallocAsync(&d_h, ncol * 4, st));
-  MESO_CUDA_TRY(cudaMallocAsync(&d_hmax, (uint64_t)bx * by * 4, st));
-  MESO_CUDA_TRY(cudaMallocAsync(&d_flags, nb, st));
-  MESO_CUDA_TRY(cudaMallocAsync(&d_ptr_tmp, nb * 4, st));
+  cudaError_t ae = cudaMallocAsync(&d_h, ncol * 4, st);
+  if (ae == cudaSuccess) ae = cudaMallocAsync(&d_hmax, (uint64_t)bx * by * 4, st);
+  if (ae == cudaSuccess) ae = cudaMallocAsync(&d_flags, nb, st);
+  if (ae == cudaSuccess) ae = cudaMallocAsync(&d_ptr_tmp, nb * 4, st);
+  if (ae != cudaSuccess) {
+    cudaFreeAsync(d_h, st);  // cudaFreeAsync(nullptr) is a no-op
+    cudaFreeAsync(d_hmax, st);
+    cudaFreeAsync(d_flags, st);
+    cudaStreamSynchronize(st);
+    return cuda_fail(ae, "terrain build: scratch allocation");
+  }
   heights_kernel<<<(unsigned)((ncol + 255) / 256), 256, 0, st>>>(T, d_h);
   column_max_kernel<<<(bx * by + 255) / 256, 256, 0, st>>>(T, d_h, d_hmax);
   terrain_brick_kernel<false><<<grid_for(nb), 256, 0, st>>>(T, d_h, d_hmax, d_flags, nullptr, nullptr, nullptr);
@@ -584,10 +591,17 @@ meso_status scene_create_dense(meso_ctx* ctx, const uint16_t* h_grid, int32_t nx
   uint16_t* d_grid = nullptr;
   uint8_t* d_flags = nullptr;
   uint32_t* d_ptr_tmp = nullptr;
-  MESO_CUDA_TRY(cudaMallocAsync(&d_grid, nvox * 2, st));
-  MESO_CUDA_TRY(cudaMallocAsync(&d_flags, nb, st));
-  MESO_CUDA_TRY(cudaMallocAsync(&d_ptr_tmp, nb * 4, st));
-  MESO_CUDA_TRY(cudaMemcpyAsync(d_grid, h_grid, nvox * 2, cudaMemcpyHostToDevice, st));
+  cudaError_t ae = cudaMallocAsync(&d_grid, nvox * 2, st);
+  if (ae == cudaSuccess) ae = cudaMallocAsync(&d_flags, nb, st);
+  if (ae == cudaSuccess) ae = cudaMallocAsync(&d_ptr_tmp, nb * 4, st);
+  if (ae == cudaSuccess) ae = cudaMemcpyAsync(d_grid, h_grid, nvox * 2, cudaMemcpyHostToDevice, st);
+  if (ae != cudaSuccess) {
+    cudaFreeAsync(d_grid, st);  // cudaFreeAsync(nullptr) is a no-op
+    cudaFreeAsync(d_flags, st);
+    cudaFreeAsync(d_ptr_tmp, st);
+    cudaStreamSynchronize(st);
+    return cuda_fail(ae, "dense scene: scratch allocation or upload");
+  }
   dense_flag_kernel<<<grid_for(nb), 256, 0, st>>>(d_grid, nx, ny, nz, d_flags);
   ctx->launches.fetch_add(1);
   uint64_t count = 0;
@@ -735,9 +749,13 @@ meso_status edit_spheres(meso_ctx* ctx, meso_scene* s, const meso_sphere_edit* h
   uint8_t* d_state = reinterpret_cast<uint8_t*>(d_temp) + nb * 1024;
   uint32_t* d_cells = reinterpret_cast<uint32_t*>(d + ((n * sizeof(meso_sphere_edit) + nb * 4 + 15) & ~size_t(15)) +
                                                   ((nb * 1024 + nb + 15) & ~size_t(15)));
-  MESO_CUDA_TRY(cudaMemcpyAsync(d_sp, h_sp, n * sizeof(meso_sphere_edit), cudaMemcpyHostToDevice, st));
-  MESO_CUDA_TRY(cudaMemcpyAsync(d_b, bricks.data(), nb * 4, cudaMemcpyHostToDevice, st));
-  MESO_CUDA_TRY(cudaMemcpyAsync(d_cells, cells.data(), nc * 4, cudaMemcpyHostToDevice, st));
+  cudaError_t ce = cudaMemcpyAsync(d_sp, h_sp, n * sizeof(meso_sphere_edit), cudaMemcpyHostToDevice, st);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_b, bricks.data(), nb * 4, cudaMemcpyHostToDevice, st);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_cells, cells.data(), nc * 4, cudaMemcpyHostToDevice, st);
+  if (ce != cudaSuccess) {
+    cudaFreeAsync(d, st);
+    return cuda_fail(ce, "edit: upload");
+  }
   EditParams P;
   P.spheres = d_sp;
   P.n_spheres = n;
@@ -759,8 +777,9 @@ meso_status edit_spheres(meso_ctx* ctx, meso_scene* s, const meso_sphere_edit* h
   edit_alloc_kernel<<<blocks, 256, 0, st>>>(P);
   edit_fix_kernel<<<1, 1, 0, st>>>(P.alloc, P.capacity);
   ctx->launches.fetch_add(3);
-  MESO_TRY(rebuild_macro(ctx, s, d_cells, (uint32_t)nc, st));
+  const meso_status mrc = rebuild_macro(ctx, s, d_cells, (uint32_t)nc, st);
   MESO_CUDA_TRY(cudaFreeAsync(d, st));
+  if (mrc != MESO_OK) return mrc;
   MESO_CUDA_TRY(cudaGetLastError());
   if (h_dirty && chunks.size() > dirty_cap) return fail(MESO_ERR_OVERFLOW, "edit: dirty list overflow");
   return MESO_OK;
