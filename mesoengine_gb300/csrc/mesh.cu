@@ -602,6 +602,11 @@ __global__ void __launch_bounds__(kThreads, 2)
         run = __shfl_sync(kFull, run, 0);
         uint32_t mine = total;
         const uint64_t chunk_bits = (uint64_t)((p.chunk_id_base + (uint32_t)c) & 0xFFFFFu) << 44;
+        if (tid == 0) prefetch_chunk<KIND>(p, &tmap, pf_a, pf_b, pf_c);
+        // the slices' rest flags are complete after this barrier; each warp
+        // then emits its own isolated quads and pulls greedy tasks as soon as
+        // it is done, so uneven emission work does not idle warps at a barrier
+        __syncthreads();
         // ---- pass 3: isolated quads of this warp's words, the 4 rows of one
         // direction at a time (lane = slice).  A warp-balanced expansion over
         // all set bits of the 4 x 32 words: lane j of round k emits the
@@ -666,8 +671,6 @@ __global__ void __launch_bounds__(kThreads, 2)
           }
           run += G;
         }
-        if (tid == 0) prefetch_chunk<KIND>(p, &tmap, pf_a, pf_b, pf_c);
-        __syncthreads();
         // ---- pass 4: greedy on the remaining faces, one warp per slice.
         // Lane r holds row r of the slice in registers: its faces (isolated
         // ones removed again), their equality with the -u and -v neighbours,
