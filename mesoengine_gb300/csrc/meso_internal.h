@@ -78,6 +78,9 @@ struct meso_scene {
   // one byte per 4x4x4-brick cell (a 32^3 chunk): nonzero iff a brick of the
   // cell is occupied; lets a ray cross an empty cell in one jump
   uint8_t* d_macro = nullptr;
+  // one byte per 16x16x16-brick cell (128^3 voxels, partial at the far
+  // edges): nonzero iff one of its 32^3 cells is, or it extends past the grid
+  uint8_t* d_macro2 = nullptr;
   uint64_t capacity = 0;       // pool slots
   // allocator state (device): [0] bump (slots ever used), [1] free-stack top
   int64_t* d_alloc = nullptr;
@@ -92,6 +95,9 @@ inline uint64_t n_bricks_of(const meso_scene* s) {
   return (uint64_t)s->bx * (uint64_t)s->by * (uint64_t)s->bz;
 }
 inline uint64_t n_macro_of(const meso_scene* s) { return n_bricks_of(s) / 64; }
+inline uint64_t n_macro2_of(const meso_scene* s) {
+  return (uint64_t)((s->bx + 15) / 16) * (uint64_t)((s->by + 15) / 16) * (uint64_t)((s->bz + 15) / 16);
+}
 
 inline cudaStream_t pick_stream(meso_ctx* ctx, void* s) {
   return s ? (cudaStream_t)s : ctx->stream;

@@ -24,7 +24,8 @@ struct RayView {
   const uint32_t* ptr;
   const uint64_t* occ;
   const uint16_t* mat;
-  const uint8_t* macro;  // per 4x4x4-brick cell: nonzero iff a brick of it is occupied
+  const uint8_t* macro;   // per 4x4x4-brick cell: nonzero iff a brick of it is occupied
+  const uint8_t* macro2;  // per 16x16x16-brick cell: nonzero iff a 4x4x4 cell of it is, or it leaves the grid
   int32_t nx, ny, nz;
   int32_t cam_chunk[3];
   float o[3];
@@ -75,24 +76,41 @@ __device__ __forceinline__ float bound_time(int b, float o, float inv) {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-// Brick steps the two-level DDA takes along axis c (sign s, brick B, next
-// brick boundary nb) while it crosses the empty 4x4x4-brick cell that B lies
-// in, up to the step that leaves the cell through axis aE at time tE.  The
-// DDA takes its boundary events in (time, axis x<y<z) order and the events of
-// one axis come at strictly increasing times, so the steps along c are its
-// interior boundaries that precede (tE, aE) in that order; along aE they are
-// all interior boundaries plus the exit itself.
-__device__ __forceinline__ int cell_steps(int c, int aE, int s, int B, int nb, float o, float inv, float tE) {
+// Brick steps the two-level DDA takes along a non-exit axis (sign s, brick
+// B, next brick boundary nb) while it crosses an empty cell of (mask+1)^3
+// bricks, up to the step that leaves the cell through another axis at time
+// tE (c_first: this axis wins ties with the exit axis).  The DDA takes its
+// boundary events in (time, axis x<y<z) order and one axis's events come at
+// strictly increasing times, so these steps are the interior boundaries that
+// precede the exit in that order: a prefix.  Its length is estimated from the
+// position at tE and settled by exact boundary-time comparisons.
+__device__ __forceinline__ int cell_steps(int s, int B, int mask, int nb, float o, float d, float inv, float tE,
+                                          bool c_first) {
   if (s == 0) return 0;
-  const int inner = s > 0 ? 3 - (B & 3) : (B & 3);
-  if (c == aE) return inner + 1;
-  int k = 0;
-  for (int j = 0; j < inner; j++) {
-    const float tj = bound_time(nb + 8 * s * j, o, inv);
-    if (tj < tE || (tj == tE && c < aE)) k++;
-    else break;
+  const int inner = s > 0 ? mask - (B & mask) : (B & mask);
+  if (inner == 0) return 0;
+  const float pos = __fmaf_rn(d, tE, o);  // an estimate only
+  const float q = s > 0 ? __fsub_rn(pos, __int2float_rn(nb)) : __fsub_rn(__int2float_rn(nb), pos);
+  int k = clampi((int)ceilf(__fmul_rn(q, 0.125f)), 0, inner);
+  while (k > 0) {
+    const float tj = bound_time(nb + 8 * s * (k - 1), o, inv);
+    if (tj < tE || (tj == tE && c_first)) break;
+    k--;
+  }
+  while (k < inner) {
+    const float tj = bound_time(nb + 8 * s * k, o, inv);
+    if (!(tj < tE || (tj == tE && c_first))) break;
+    k++;
   }
   return k;
+}
+
+// Empty-cell level of brick B: 2 if its 16^3-brick cell is empty, 1 if its
+// 4^3-brick cell is, else 0 (both bytes are fetched together).
+__device__ __forceinline__ int cell_level(const RayView& V, int Bx, int By, int Bz, int MX, int MY, int MX2, int MY2) {
+  const uint8_t m2 = __ldg(V.macro2 + (Bx >> 4) + MX2 * ((By >> 4) + MY2 * (Bz >> 4)));
+  const uint8_t m1 = __ldg(V.macro + (Bx >> 2) + MX * ((By >> 2) + MY * (Bz >> 2)));
+  return m2 == 0 ? 2 : (m1 == 0 ? 1 : 0);
 }
 
 // Walks from voxel (vx,vy,vz) (absolute, inside the grid) at time t, entered
@@ -115,7 +133,8 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
   const int sz = dz > 0.0f ? 1 : (dz < 0.0f ? -1 : 0);
   const int px = sx > 0 ? 1 : 0, py = sy > 0 ? 1 : 0, pz = sz > 0 ? 1 : 0;
   const int NBx = V.nx >> 3, NBy = V.ny >> 3, NBz = V.nz >> 3;
-  const int MX = NBx >> 2, MY = NBy >> 2;  // cells of 4x4x4 bricks
+  const int MX = NBx >> 2, MY = NBy >> 2;                  // cells of 4x4x4 bricks
+  const int MX2 = (NBx + 15) >> 4, MY2 = (NBy + 15) >> 4;  // cells of 16x16x16 bricks
   const uint32_t strideY = (uint32_t)NBx, strideZ = (uint32_t)NBx * (uint32_t)NBy;
   // signed index increments of one step along each axis
   const uint32_t dIx = (uint32_t)sx, dIy = (uint32_t)(sy * (int)strideY), dIz = (uint32_t)(sz * (int)strideZ);
@@ -142,21 +161,28 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
       float tz = sz ? bound_time(nbz, oz, iz) : kInf;
       bool out = false;
       int a = ea;
-      bool empty_cell = !kStats && __ldg(V.macro + (Bx >> 2) + MX * ((By >> 2) + MY * (Bz >> 2))) == 0;
+      // cell level at the current brick: 2 = its 16^3-brick cell is empty,
+      // 1 = its 4^3-brick cell is empty, 0 = take brick steps
+      int lvl = 0;
+      if (!kStats) lvl = cell_level(V, Bx, By, Bz, MX, MY, MX2, MY2);
       bool stale = false;
       for (;;) {
-        if (empty_cell) {
-          const float Tx = sx ? bound_time(((Bx >> 2) + px) * 32 - bx0, ox, ix) : kInf;
-          const float Ty = sy ? bound_time(((By >> 2) + py) * 32 - by0, oy, iy) : kInf;
-          const float Tz = sz ? bound_time(((Bz >> 2) + pz) * 32 - bz0, oz, iz) : kInf;
+        if (lvl) {
+          const int sh = lvl == 2 ? 4 : 2, mask = (1 << sh) - 1;
+          const float Tx = sx ? bound_time((((Bx >> sh) + px) << (sh + 3)) - bx0, ox, ix) : kInf;
+          const float Ty = sy ? bound_time((((By >> sh) + py) << (sh + 3)) - by0, oy, iy) : kInf;
+          const float Tz = sz ? bound_time((((Bz >> sh) + pz) << (sh + 3)) - bz0, oz, iz) : kInf;
           const bool my = Ty < Tx;
           float tE = my ? Ty : Tx;
           const bool mz = Tz < tE;
           tE = mz ? Tz : tE;
           const int aE = mz ? 2 : (my ? 1 : 0);
-          const int kx = cell_steps(0, aE, sx, Bx, nbx, ox, ix, tE);
-          const int ky = cell_steps(1, aE, sy, By, nby, oy, iy, tE);
-          const int kz = cell_steps(2, aE, sz, Bz, nbz, oz, iz, tE);
+          // along the exit axis every brick up to the face, then the exit step
+          const int Be = aE == 0 ? Bx : (aE == 1 ? By : Bz), se = aE == 0 ? sx : (aE == 1 ? sy : sz);
+          const int ke = (se > 0 ? mask - (Be & mask) : (Be & mask)) + 1;
+          const int kx = aE == 0 ? ke : cell_steps(sx, Bx, mask, nbx, ox, dx, ix, tE, true);
+          const int ky = aE == 1 ? ke : cell_steps(sy, By, mask, nby, oy, dy, iy, tE, aE == 2);
+          const int kz = aE == 2 ? ke : cell_steps(sz, Bz, mask, nbz, oz, dz, iz, tE, false);
           const uint32_t k = (uint32_t)(kx + ky + kz);
           if (cs + fs + k <= cap) {
             cs += k;
@@ -173,11 +199,11 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
             out = ((unsigned)Bx >= (unsigned)NBx) | ((unsigned)By >= (unsigned)NBy) | ((unsigned)Bz >= (unsigned)NBz);
             if (out || cs + fs > cap) break;
             p = __ldg(V.ptr + idx);
-            empty_cell = __ldg(V.macro + (Bx >> 2) + MX * ((By >> 2) + MY * (Bz >> 2))) == 0;
+            lvl = cell_level(V, Bx, By, Bz, MX, MY, MX2, MY2);
             if (p != MESO_EMPTY_BRICK) break;
             continue;
           }
-          empty_cell = false;  // the jump would pass the step cap: take brick steps
+          lvl = 0;  // the jump would pass the step cap: take brick steps
         }
         if (stale) {
           tx = sx ? bound_time(nbx, ox, ix) : kInf;
@@ -207,8 +233,7 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
           // entering a new cell: is it empty?
           const int cnew = a0 ? Bx : (a1 ? By : Bz);
           const int snew = a0 ? sx : (a1 ? sy : sz);
-          if ((cnew & 3) == (snew > 0 ? 0 : 3))
-            empty_cell = __ldg(V.macro + (Bx >> 2) + MX * ((By >> 2) + MY * (Bz >> 2))) == 0;
+          if ((cnew & 3) == (snew > 0 ? 0 : 3)) lvl = cell_level(V, Bx, By, Bz, MX, MY, MX2, MY2);
         }
         // the next boundary time is computed while the pointer load is in
         // flight; an occupied brick recomputes its times from scratch
@@ -508,6 +533,7 @@ static uint64_t fill_views(const meso_scene* const* scenes, const meso_camera* c
     memset(&V, 0, sizeof(V));
     V.ptr = s->d_ptr;
     V.macro = s->d_macro;
+    V.macro2 = s->d_macro2;
     V.occ = s->d_occ;
     V.mat = s->d_mat;
     V.nx = s->nx;

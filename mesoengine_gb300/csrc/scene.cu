@@ -448,6 +448,22 @@ __global__ void macro_kernel(const uint32_t* ptr, int bx, int by, uint8_t* macro
   if (lane == 0) macro[m] = occupied ? 1 : 0;
 }
 
+// One thread per 16x16x16-brick cell: any occupied 4x4x4-brick child -> 1; a
+// cell that extends past the grid is marked 1 too, so no jump leaves the grid.
+__global__ void macro2_kernel(const uint8_t* macro, int bx, int by, int bz, uint8_t* macro2) {
+  const int m2x = (bx + 15) / 16, m2y = (by + 15) / 16, m2z = (bz + 15) / 16;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)(m2x * m2y * m2z)) return;
+  const int cx = (int)(i % (uint32_t)m2x), cy = (int)((i / (uint32_t)m2x) % (uint32_t)m2y), cz = (int)(i / ((uint32_t)m2x * m2y));
+  const int mx = bx / 4, my = by / 4, mz = bz / 4;
+  bool any = (cx + 1) * 4 > mx || (cy + 1) * 4 > my || (cz + 1) * 4 > mz;
+  for (int k = 0; k < 64 && !any; k++) {
+    const int x = cx * 4 + (k & 3), y = cy * 4 + ((k >> 2) & 3), z = cz * 4 + (k >> 4);
+    any = macro[(uint32_t)x + (uint32_t)mx * ((uint32_t)y + (uint32_t)my * (uint32_t)z)] != 0;
+  }
+  macro2[i] = any ? 1 : 0;
+}
+
 // ---------------------------------------------------------------- scene API
 
 meso_status scene_alloc(meso_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, uint64_t capacity, meso_scene** out) {
@@ -460,7 +476,7 @@ meso_status scene_alloc(meso_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, uint6
   s->bz = nz / 8;
   s->capacity = capacity;
   const uint64_t nb = n_bricks_of(s);
-  const uint64_t bytes = nb * 4 + nb / 64 + capacity * (64 + 1024 + 4) + 16;
+  const uint64_t bytes = nb * 4 + nb / 64 + n_macro2_of(s) + capacity * (64 + 1024 + 4) + 16;
   if (ctx->budget_bytes && ctx->scene_bytes.load() + bytes > ctx->budget_bytes) {
     delete s;
     return fail(MESO_ERR_OVER_BUDGET, "scene exceeds the HBM budget");
@@ -468,6 +484,8 @@ meso_status scene_alloc(meso_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, uint6
   cudaError_t e = cudaMalloc(&s->d_ptr, nb * 4);
   if (e == cudaSuccess) e = cudaMalloc(&s->d_macro, std::max<uint64_t>(nb / 64, 1));
   if (e == cudaSuccess) e = cudaMemset(s->d_macro, 0, std::max<uint64_t>(nb / 64, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_macro2, std::max<uint64_t>(n_macro2_of(s), 1));
+  if (e == cudaSuccess) e = cudaMemset(s->d_macro2, 1, std::max<uint64_t>(n_macro2_of(s), 1));
   if (e == cudaSuccess) e = cudaMalloc(&s->d_occ, std::max<uint64_t>(capacity, 1) * 64);
   if (e == cudaSuccess) e = cudaMalloc(&s->d_mat, std::max<uint64_t>(capacity, 1) * 1024);
   if (e == cudaSuccess) e = cudaMalloc(&s->d_free, std::max<uint64_t>(capacity, 1) * 4);
@@ -488,6 +506,7 @@ void scene_release(meso_ctx* ctx, meso_scene* s) {
   if (!s) return;
   cudaFree(s->d_ptr);
   cudaFree(s->d_macro);
+  cudaFree(s->d_macro2);
   cudaFree(s->d_occ);
   cudaFree(s->d_mat);
   cudaFree(s->d_free);
@@ -501,7 +520,9 @@ meso_status rebuild_macro(meso_ctx* ctx, meso_scene* s, const uint32_t* d_cells,
   if (cells == 0) return MESO_OK;
   macro_kernel<<<(unsigned)((cells * 32 + 255) / 256), 256, 0, st>>>(s->d_ptr, s->bx, s->by, s->d_macro, d_cells,
                                                                      cells);
-  ctx->launches.fetch_add(1);
+  const uint64_t cells2 = n_macro2_of(s);
+  macro2_kernel<<<(unsigned)((cells2 + 255) / 256), 256, 0, st>>>(s->d_macro, s->bx, s->by, s->bz, s->d_macro2);
+  ctx->launches.fetch_add(2);
   MESO_CUDA_TRY(cudaGetLastError());
   return MESO_OK;
 }
