@@ -471,15 +471,6 @@ __device__ __forceinline__ void trace_pixel(const RayView& V, uint32_t px, uint3
   h.shadow_steps = sr.fine | (sr.coarse << 16);
 }
 
-__device__ __forceinline__ void store_hit(meso_hit* dst, const meso_hit& h) {
-  uint64_t* d = reinterpret_cast<uint64_t*>(dst);
-  const uint64_t w1 = (uint64_t)__float_as_uint(h.t) | (uint64_t)h.material << 32 | (uint64_t)h.face << 48 |
-                      (uint64_t)h.shadow << 56;
-  const uint64_t w2 = (uint64_t)h.steps | (uint64_t)h.shadow_steps << 32;
-  d[0] = h.voxel;
-  d[1] = w1;
-  d[2] = w2;
-}
 
 // kStats: also accumulates {pointer fetches, occupied bricks entered, hits,
 // rays} into P.stats (a separate instantiation; the timed path has none of it).
@@ -502,13 +493,33 @@ __global__ void __launch_bounds__(128, 8) raymarch_kernel(const RayParams P, con
   const RayView& V = views[lo];
   const uint32_t lt = tile - V.tile_start;
   const uint32_t tx = lt % V.tiles_x, ty = lt / V.tiles_x;
-  const uint32_t px = tx * P.tile_w + (uint32_t)lane % P.tile_w;
-  const uint32_t py = ty * P.tile_h + (uint32_t)lane / P.tile_w;
+  const uint32_t px0 = tx * P.tile_w, py0 = ty * P.tile_h;
+  const uint32_t px = px0 + (uint32_t)lane % P.tile_w;
+  const uint32_t py = py0 + (uint32_t)lane / P.tile_w;
   uint32_t st[4] = {0, 0, 0, 0};
+  // The tile's hit records (24 B each) are staged in shared memory and
+  // written back as runs of consecutive 8-byte words, one run per tile row,
+  // so every store instruction fills whole sectors (this matters most when
+  // the output is page-locked host memory written over the CPU-GPU link).
+  __shared__ uint64_t stage[4][96];
+  uint64_t* sw = stage[threadIdx.x >> 5];
   if (px < V.width && py < V.height) {
     meso_hit h;
     trace_pixel<kStats>(V, px, py, P, h, st);
-    store_hit(P.hits + V.hit_offset + (uint64_t)py * V.width + px, h);
+    sw[3 * lane] = h.voxel;
+    sw[3 * lane + 1] = (uint64_t)__float_as_uint(h.t) | (uint64_t)h.material << 32 | (uint64_t)h.face << 48 |
+                       (uint64_t)h.shadow << 56;
+    sw[3 * lane + 2] = (uint64_t)h.steps | (uint64_t)h.shadow_steps << 32;
+  }
+  __syncwarp();
+  const uint32_t row_words = 3 * P.tile_w;
+  uint64_t* base = reinterpret_cast<uint64_t*>(P.hits + V.hit_offset);
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+    const uint32_t c = (uint32_t)lane + 32u * r;  // word c of the tile: row c / row_words
+    const uint32_t row = c / row_words, w = c % row_words;
+    const uint32_t x = px0 + w / 3, y = py0 + row;
+    if (x < V.width && y < V.height) base[((uint64_t)y * V.width + px0) * 3 + w] = sw[c];
   }
   if (kStats) {
     for (int k = 0; k < 4; k++) {
