@@ -81,6 +81,8 @@ struct meso_scene {
   // one byte per 16x16x16-brick cell (128^3 voxels, partial at the far
   // edges): nonzero iff one of its 32^3 cells is, or it extends past the grid
   uint8_t* d_macro2 = nullptr;
+  // one byte per 64x64x64-brick cell (512^3 voxels), built like d_macro2 from it
+  uint8_t* d_macro3 = nullptr;
   uint64_t capacity = 0;       // pool slots
   // allocator state (device): [0] bump (slots ever used), [1] free-stack top
   int64_t* d_alloc = nullptr;
@@ -97,6 +99,9 @@ inline uint64_t n_bricks_of(const meso_scene* s) {
 inline uint64_t n_macro_of(const meso_scene* s) { return n_bricks_of(s) / 64; }
 inline uint64_t n_macro2_of(const meso_scene* s) {
   return (uint64_t)((s->bx + 15) / 16) * (uint64_t)((s->by + 15) / 16) * (uint64_t)((s->bz + 15) / 16);
+}
+inline uint64_t n_macro3_of(const meso_scene* s) {
+  return (uint64_t)((s->bx + 63) / 64) * (uint64_t)((s->by + 63) / 64) * (uint64_t)((s->bz + 63) / 64);
 }
 
 inline cudaStream_t pick_stream(meso_ctx* ctx, void* s) {

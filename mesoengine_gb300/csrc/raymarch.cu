@@ -26,6 +26,7 @@ struct RayView {
   const uint16_t* mat;
   const uint8_t* macro;   // per 4x4x4-brick cell: nonzero iff a brick of it is occupied
   const uint8_t* macro2;  // per 16x16x16-brick cell: nonzero iff a 4x4x4 cell of it is, or it leaves the grid
+  const uint8_t* macro3;  // per 64x64x64-brick cell, likewise from the 16x16x16 cells
   int32_t nx, ny, nz;
   int32_t cam_chunk[3];
   float o[3];
@@ -105,12 +106,15 @@ __device__ __forceinline__ int cell_steps(int s, int B, int mask, int nb, float 
   return k;
 }
 
-// Empty-cell level of brick B: 2 if its 16^3-brick cell is empty, 1 if its
-// 4^3-brick cell is, else 0 (both bytes are fetched together).
-__device__ __forceinline__ int cell_level(const RayView& V, int Bx, int By, int Bz, int MX, int MY, int MX2, int MY2) {
+// Empty-cell level of brick B: 3 if its 64^3-brick cell is empty, 2 if its
+// 16^3-brick cell is, 1 if its 4^3-brick cell is, else 0 (the three bytes
+// are fetched together).
+__device__ __forceinline__ int cell_level(const RayView& V, int Bx, int By, int Bz, int MX, int MY, int MX2, int MY2,
+                                          int MX3, int MY3) {
+  const uint8_t m3 = __ldg(V.macro3 + (Bx >> 6) + MX3 * ((By >> 6) + MY3 * (Bz >> 6)));
   const uint8_t m2 = __ldg(V.macro2 + (Bx >> 4) + MX2 * ((By >> 4) + MY2 * (Bz >> 4)));
   const uint8_t m1 = __ldg(V.macro + (Bx >> 2) + MX * ((By >> 2) + MY * (Bz >> 2)));
-  return m2 == 0 ? 2 : (m1 == 0 ? 1 : 0);
+  return m3 == 0 ? 3 : (m2 == 0 ? 2 : (m1 == 0 ? 1 : 0));
 }
 
 // Walks from voxel (vx,vy,vz) (absolute, inside the grid) at time t, entered
@@ -135,6 +139,7 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
   const int NBx = V.nx >> 3, NBy = V.ny >> 3, NBz = V.nz >> 3;
   const int MX = NBx >> 2, MY = NBy >> 2;                  // cells of 4x4x4 bricks
   const int MX2 = (NBx + 15) >> 4, MY2 = (NBy + 15) >> 4;  // cells of 16x16x16 bricks
+  const int MX3 = (NBx + 63) >> 6, MY3 = (NBy + 63) >> 6;  // cells of 64x64x64 bricks
   const uint32_t strideY = (uint32_t)NBx, strideZ = (uint32_t)NBx * (uint32_t)NBy;
   // signed index increments of one step along each axis
   const uint32_t dIx = (uint32_t)sx, dIy = (uint32_t)(sy * (int)strideY), dIz = (uint32_t)(sz * (int)strideZ);
@@ -161,14 +166,14 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
       float tz = sz ? bound_time(nbz, oz, iz) : kInf;
       bool out = false;
       int a = ea;
-      // cell level at the current brick: 2 = its 16^3-brick cell is empty,
-      // 1 = its 4^3-brick cell is empty, 0 = take brick steps
+      // cell level at the current brick: 3 / 2 / 1 = its 64^3- / 16^3- /
+      // 4^3-brick cell is empty (the largest such), 0 = take brick steps
       int lvl = 0;
-      if (!kStats) lvl = cell_level(V, Bx, By, Bz, MX, MY, MX2, MY2);
+      if (!kStats) lvl = cell_level(V, Bx, By, Bz, MX, MY, MX2, MY2, MX3, MY3);
       bool stale = false;
       for (;;) {
         if (lvl) {
-          const int sh = lvl == 2 ? 4 : 2, mask = (1 << sh) - 1;
+          const int sh = 2 * lvl, mask = (1 << sh) - 1;
           const float Tx = sx ? bound_time((((Bx >> sh) + px) << (sh + 3)) - bx0, ox, ix) : kInf;
           const float Ty = sy ? bound_time((((By >> sh) + py) << (sh + 3)) - by0, oy, iy) : kInf;
           const float Tz = sz ? bound_time((((Bz >> sh) + pz) << (sh + 3)) - bz0, oz, iz) : kInf;
@@ -199,7 +204,7 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
             out = ((unsigned)Bx >= (unsigned)NBx) | ((unsigned)By >= (unsigned)NBy) | ((unsigned)Bz >= (unsigned)NBz);
             if (out || cs + fs > cap) break;
             p = __ldg(V.ptr + idx);
-            lvl = cell_level(V, Bx, By, Bz, MX, MY, MX2, MY2);
+            lvl = cell_level(V, Bx, By, Bz, MX, MY, MX2, MY2, MX3, MY3);
             if (p != MESO_EMPTY_BRICK) break;
             continue;
           }
@@ -233,7 +238,7 @@ __device__ __forceinline__ void traverse(const RayView& V, int bx0, int by0, int
           // entering a new cell: is it empty?
           const int cnew = a0 ? Bx : (a1 ? By : Bz);
           const int snew = a0 ? sx : (a1 ? sy : sz);
-          if ((cnew & 3) == (snew > 0 ? 0 : 3)) lvl = cell_level(V, Bx, By, Bz, MX, MY, MX2, MY2);
+          if ((cnew & 3) == (snew > 0 ? 0 : 3)) lvl = cell_level(V, Bx, By, Bz, MX, MY, MX2, MY2, MX3, MY3);
         }
         // the next boundary time is computed while the pointer load is in
         // flight; an occupied brick recomputes its times from scratch
@@ -545,6 +550,7 @@ static uint64_t fill_views(const meso_scene* const* scenes, const meso_camera* c
     V.ptr = s->d_ptr;
     V.macro = s->d_macro;
     V.macro2 = s->d_macro2;
+    V.macro3 = s->d_macro3;
     V.occ = s->d_occ;
     V.mat = s->d_mat;
     V.nx = s->nx;

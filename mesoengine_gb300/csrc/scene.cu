@@ -464,6 +464,23 @@ __global__ void macro2_kernel(const uint8_t* macro, int bx, int by, int bz, uint
   macro2[i] = any ? 1 : 0;
 }
 
+// One thread per 64x64x64-brick cell: any nonzero 16x16x16 child, or a cell
+// extending past the grid -> 1.
+__global__ void macro3_kernel(const uint8_t* macro2, int bx, int by, int bz, uint8_t* macro3) {
+  const int m3x = (bx + 63) / 64, m3y = (by + 63) / 64, m3z = (bz + 63) / 64;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)(m3x * m3y * m3z)) return;
+  const int cx = (int)(i % (uint32_t)m3x), cy = (int)((i / (uint32_t)m3x) % (uint32_t)m3y), cz = (int)(i / ((uint32_t)m3x * m3y));
+  const int m2x = (bx + 15) / 16, m2y = (by + 15) / 16, m2z = (bz + 15) / 16;
+  bool any = (cx + 1) * 64 > bx || (cy + 1) * 64 > by || (cz + 1) * 64 > bz;
+  for (int k = 0; k < 64 && !any; k++) {
+    const int x = cx * 4 + (k & 3), y = cy * 4 + ((k >> 2) & 3), z = cz * 4 + (k >> 4);
+    any = macro2[(uint32_t)x + (uint32_t)m2x * ((uint32_t)y + (uint32_t)m2y * (uint32_t)z)] != 0;
+  }
+  (void)m2z;
+  macro3[i] = any ? 1 : 0;
+}
+
 // ---------------------------------------------------------------- scene API
 
 meso_status scene_alloc(meso_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, uint64_t capacity, meso_scene** out) {
@@ -476,7 +493,7 @@ meso_status scene_alloc(meso_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, uint6
   s->bz = nz / 8;
   s->capacity = capacity;
   const uint64_t nb = n_bricks_of(s);
-  const uint64_t bytes = nb * 4 + nb / 64 + n_macro2_of(s) + capacity * (64 + 1024 + 4) + 16;
+  const uint64_t bytes = nb * 4 + nb / 64 + n_macro2_of(s) + n_macro3_of(s) + capacity * (64 + 1024 + 4) + 16;
   if (ctx->budget_bytes && ctx->scene_bytes.load() + bytes > ctx->budget_bytes) {
     delete s;
     return fail(MESO_ERR_OVER_BUDGET, "scene exceeds the HBM budget");
@@ -486,6 +503,8 @@ meso_status scene_alloc(meso_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, uint6
   if (e == cudaSuccess) e = cudaMemset(s->d_macro, 0, std::max<uint64_t>(nb / 64, 1));
   if (e == cudaSuccess) e = cudaMalloc(&s->d_macro2, std::max<uint64_t>(n_macro2_of(s), 1));
   if (e == cudaSuccess) e = cudaMemset(s->d_macro2, 1, std::max<uint64_t>(n_macro2_of(s), 1));
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_macro3, std::max<uint64_t>(n_macro3_of(s), 1));
+  if (e == cudaSuccess) e = cudaMemset(s->d_macro3, 1, std::max<uint64_t>(n_macro3_of(s), 1));
   if (e == cudaSuccess) e = cudaMalloc(&s->d_occ, std::max<uint64_t>(capacity, 1) * 64);
   if (e == cudaSuccess) e = cudaMalloc(&s->d_mat, std::max<uint64_t>(capacity, 1) * 1024);
   if (e == cudaSuccess) e = cudaMalloc(&s->d_free, std::max<uint64_t>(capacity, 1) * 4);
@@ -507,6 +526,7 @@ void scene_release(meso_ctx* ctx, meso_scene* s) {
   cudaFree(s->d_ptr);
   cudaFree(s->d_macro);
   cudaFree(s->d_macro2);
+  cudaFree(s->d_macro3);
   cudaFree(s->d_occ);
   cudaFree(s->d_mat);
   cudaFree(s->d_free);
@@ -522,7 +542,9 @@ meso_status rebuild_macro(meso_ctx* ctx, meso_scene* s, const uint32_t* d_cells,
                                                                      cells);
   const uint64_t cells2 = n_macro2_of(s);
   macro2_kernel<<<(unsigned)((cells2 + 255) / 256), 256, 0, st>>>(s->d_macro, s->bx, s->by, s->bz, s->d_macro2);
-  ctx->launches.fetch_add(2);
+  const uint64_t cells3 = n_macro3_of(s);
+  macro3_kernel<<<(unsigned)((cells3 + 255) / 256), 256, 0, st>>>(s->d_macro2, s->bx, s->by, s->bz, s->d_macro3);
+  ctx->launches.fetch_add(3);
   MESO_CUDA_TRY(cudaGetLastError());
   return MESO_OK;
 }

@@ -173,6 +173,24 @@ def test_empty_cell_map_follows_edits(ctx, sparse):
         assert_hits_equal(ctx.raymarch(scene, cam), oracle.raymarch(bm, oracle.camera(o, tg, 64, 48)))
 
 
+def test_all_cell_levels_match_oracle(ctx):
+    # 1024 x 512 x 1024 terrain below z ~ 300: the 512^3-voxel cells above
+    # z = 512 are empty, so rays take jumps of every size (512^3, 128^3 and
+    # 32^3 voxels) and brick steps; the oracle walks brick by brick over the
+    # same arrays copied back from the device
+    t = meso.Terrain(1024, 512, 1024, 21, 256, 6, 40.0, 200.0, 48, 0.7)
+    scene = ctx.scene_from_terrain(t)
+    ptr, occ, mat = scene.download()
+    bm = oracle.HostBrickMap.from_arrays((1024, 512, 1024), ptr, occ, mat)
+    poses = [((-200.0, -100.0, 1100.0), (600.0, 300.0, 100.0)), ((512.0, 256.0, 1500.0), (512.0, 257.0, 0.0)),
+             ((1300.0, 700.0, 900.0), (-100.0, -50.0, 700.0)), ((10.0, 10.0, 1000.0), (1000.0, 500.0, 20.0)),
+             ((-300.0, 256.0, 512.0), (1400.0, 256.0, 512.0))]
+    for o, tg in poses:
+        cam = meso.camera(o, tg, 64, 48)
+        assert_hits_equal(ctx.raymarch(scene, cam), oracle.raymarch(bm, oracle.camera(o, tg, 64, 48)))
+    scene.destroy()
+
+
 def test_matches_golden_fixture(ctx, small):
     import os
     golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
