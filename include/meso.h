@@ -242,7 +242,11 @@ typedef struct meso_hit {
 /* Marches every pixel of n_views cameras in ONE launch; view v reads scene
  * scenes[v] and writes its width*height hits after those of views 0..v-1.
  * Replaces the imposter draw (Samples/SimpleVoxel.cpp:374-393, vertex shader
- * :146-192).  light: normalised direction towards the light (MESO_RAY_SHADOW). */
+ * :146-192).  light: normalised direction towards the light (MESO_RAY_SHADOW).
+ * The walk is the two-level DDA (a coarse step per empty brick, a fine step
+ * per voxel of an occupied brick); empty cells of 4^3, 16^3 and 64^3 bricks
+ * are crossed in one jump whose result, step counts included, is that of the
+ * brick-by-brick walk. */
 meso_status meso_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* h_cams,
                           uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
                           void* stream);
@@ -258,10 +262,11 @@ meso_status meso_raymarch_per_view(meso_ctx* ctx, const meso_scene* const* scene
 meso_status meso_raymarch_host(meso_ctx* ctx, const meso_scene* scene, const meso_camera* h_cam,
                                const float light[3], uint32_t flags, meso_hit* h_hits);
 
-/* Same launch as meso_raymarch (at most 32 views) through a separate kernel
- * instantiation that also counts, over all primary and shadow rays:
- * h_counts[0] brick-pointer fetches, [1] occupied bricks entered, [2] hits,
- * [3] rays.  For roofline accounting; the timed path carries no counters. */
+/* Same launch and results as meso_raymarch (at most 32 views) through a
+ * separate kernel instantiation that takes every brick step (no cell jumps)
+ * and counts, over all primary and shadow rays: h_counts[0] brick-pointer
+ * fetches, [1] occupied bricks entered, [2] hits, [3] rays.  For roofline
+ * accounting; the timed path carries no counters. */
 meso_status meso_raymarch_stats(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* h_cams,
                                 uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
                                 uint64_t h_counts[4]);
