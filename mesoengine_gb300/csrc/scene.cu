@@ -471,13 +471,12 @@ __global__ void macro3_kernel(const uint8_t* macro2, int bx, int by, int bz, uin
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint32_t)(m3x * m3y * m3z)) return;
   const int cx = (int)(i % (uint32_t)m3x), cy = (int)((i / (uint32_t)m3x) % (uint32_t)m3y), cz = (int)(i / ((uint32_t)m3x * m3y));
-  const int m2x = (bx + 15) / 16, m2y = (by + 15) / 16, m2z = (bz + 15) / 16;
+  const int m2x = (bx + 15) / 16, m2y = (by + 15) / 16;
   bool any = (cx + 1) * 64 > bx || (cy + 1) * 64 > by || (cz + 1) * 64 > bz;
   for (int k = 0; k < 64 && !any; k++) {
     const int x = cx * 4 + (k & 3), y = cy * 4 + ((k >> 2) & 3), z = cz * 4 + (k >> 4);
     any = macro2[(uint32_t)x + (uint32_t)m2x * ((uint32_t)y + (uint32_t)m2y * (uint32_t)z)] != 0;
   }
-  (void)m2z;
   macro3[i] = any ? 1 : 0;
 }
 
