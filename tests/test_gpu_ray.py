@@ -173,6 +173,31 @@ def test_empty_cell_map_follows_edits(ctx, sparse):
         assert_hits_equal(ctx.raymarch(scene, cam), oracle.raymarch(bm, oracle.camera(o, tg, 64, 48)))
 
 
+def test_many_views_of_two_scenes_match_oracle(ctx, small, sparse):
+    # 40 views (more than the 32 passed as kernel parameters, so the view
+    # table in device memory is used) of two scenes of different sizes in
+    # one launch; every view against the oracle of its scene
+    t, s_small, bm_small = small
+    s_sparse, bm_sparse = sparse
+    rng = np.random.default_rng(23)
+    scenes, cams, refs = [], [], []
+    for i in range(40):
+        big = i % 2 == 1
+        dims = (256, 192, 128) if big else (128, 128, 128)
+        o = tuple(rng.uniform(-120, 380, 3))
+        tg = tuple(rng.uniform(0, dims))
+        w, h = int(rng.integers(8, 48)), int(rng.integers(8, 40))
+        scenes.append(s_sparse if big else s_small)
+        cams.append(meso.camera(o, tg, w, h))
+        refs.append(oracle.raymarch(bm_sparse if big else bm_small, oracle.camera(o, tg, w, h)))
+    got = ctx.raymarch(scenes, cams)
+    off = 0
+    for c, ref in zip(cams, refs):
+        n = c.width * c.height
+        assert_hits_equal(got[off:off + n], ref)
+        off += n
+
+
 def test_all_cell_levels_match_oracle(ctx):
     # 1024 x 512 x 1024 terrain below z ~ 300: the 512^3-voxel cells above
     # z = 512 are empty, so rays take jumps of every size (512^3, 128^3 and
