@@ -19,6 +19,7 @@ LIB_PATH = _build.LIB
 EMPTY_BRICK = 0xFFFFFFFF
 SRC_GRID_U8, SRC_CHUNKS_U16, SRC_BRICKMAP, SRC_GRID_U16, SRC_CHUNKS_U8 = 0, 1, 2, 3, 4
 RAY_SHADOW = 1
+MAX_CHUNKS_PER_CALL = 1 << 20
 REQ_RENDER, REQ_EDIT_REMESH_RENDER = 0, 1
 
 STATUS = {
