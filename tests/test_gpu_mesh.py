@@ -38,6 +38,46 @@ def test_kat_chunks_u16(ctx):
     assert per[0] == 6 and per[1] == 6 and per[2] == 6 * 16384
 
 
+def _component_chunks():
+    """Patterns built to exercise the order-independent peeling: isolated
+    faces, two-face components (dominoes, both orientations), L- and
+    T-shaped three- and four-face components, long runs, and the extreme
+    material values 1 and 65535."""
+    rng = np.random.default_rng(77)
+    z, y, x = np.indices((32, 32, 32))
+    c = np.zeros((12, 32, 32, 32), np.uint16)
+    # dominoes along x and along y on a sparse lattice, distinct materials
+    c[0] = np.where((x % 4 < 2) & (y % 3 == 0) & (z % 3 == 0), 1 + (x // 4 + 7 * y + 31 * z) % 60000, 0)
+    c[1] = np.where((y % 4 < 2) & (x % 3 == 0) & (z % 3 == 0), 1 + (y // 4 + 7 * x + 31 * z) % 60000, 0)
+    # vertical dominoes (two voxels along z) and L-shapes
+    c[2] = np.where((z % 4 < 2) & (x % 3 == 0) & (y % 3 == 0), 65535, 0)
+    c[3] = np.where(((x % 5 == 0) & (y % 5 < 2) | (x % 5 < 2) & (y % 5 == 0)) & (z % 4 == 1), 5, 0)
+    # random materials from a small palette on random occupancy
+    for k, (p, m) in enumerate([(0.05, 2), (0.3, 2), (0.6, 3), (0.9, 1)]):
+        occ = rng.random((32, 32, 32)) < p
+        c[4 + k] = np.where(occ, rng.integers(1, m + 1, (32, 32, 32)), 0)
+    # full slabs with a stripe of another material, and a hollow box
+    c[8] = np.where(z < 16, 1 + (x == 10) * 65534, 0)
+    c[9] = np.where((x > 2) & (x < 29) & (y > 2) & (y < 29) & (z > 2) & (z < 29), 4, 0)
+    c[9][5:27, 5:27, 5:27] = 0
+    # alternating 2-wide bands (domino-rich) and a sparse mix of everything
+    c[10] = np.where(((x // 2 + y // 2 + z) % 2 == 0), 1 + ((x // 2) % 2), 0)
+    c[11] = np.where(rng.random((32, 32, 32)) < 0.15, rng.integers(1, 65536, (32, 32, 32)), 0)
+    return c
+
+
+def test_component_patterns_match_oracle(ctx):
+    c = _component_chunks()
+    ref = oracle.mesh_chunks(oracle.SRC_CHUNKS_U16, c)
+    q, counts = ctx.mesh(meso.SRC_CHUNKS_U16, ctx.to_device(c), n=c.shape[0], chunk_counts=True)
+    assert np.array_equal(_sorted(q), ref)
+    assert np.array_equal(counts, np.bincount(oracle.unpack_quads(ref)["chunk"], minlength=c.shape[0]))
+    # the same chunks through the uint8 path (materials folded into 1..255)
+    c8 = np.where(c > 0, 1 + (c.astype(np.uint32) % 255), 0).astype(np.uint8)
+    q8, _ = ctx.mesh(meso.SRC_CHUNKS_U8, ctx.to_device(c8), n=c8.shape[0])
+    assert np.array_equal(_sorted(q8), oracle.mesh_chunks(oracle.SRC_CHUNKS_U8, c8))
+
+
 def test_generated_chunks_match_oracle(ctx):
     n = 48
     dev, solid = ctx.generate_chunks_u16(n, seed0=1)
