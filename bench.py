@@ -5,9 +5,21 @@ Headline step (value): one 1920x1080 frame of the 1024^3 sparse terrain scene
 (8^3 bricks under a 128^3 pointer grid, ~15% solid, uint16 materials),
 primary rays plus one shadow ray per hit towards normalize(0.3, 0.5, 0.8),
 FP32, one plain per-view launch; metric Mrays/s = (primary + shadow rays) / s.
-Also reported on the same line: batched meshing of 4096 standalone 32^3
-uint16 chunks (Gvox/s, persistent kernel vs one launch per chunk), and the
-served raymarch stream (p50/p99 latency, Mrays/s) when available.
+Also reported on the same line:
+  mesh        batched meshing of 4096 standalone 32^3 uint16 chunks (Gvox/s,
+              persistent kernel vs one launch per chunk, HBM roofline, CPU
+              oracle on the host cores with a bit-exact check);
+  served      the served raymarch stream: p50/p99 latency and Mrays/s at the
+              offered load, capacity (requests submitted at once) and the
+              plain form (one launch per request, waited for);
+  served_edit the served edit+remesh+render stream: p50/p99, capacity and
+              plain form in requests/s; gvox_meshed_s_wall = voxels of the
+              dirty chunks per second of the run, gvox_meshed_s_busy = the
+              same per second of request processing (edit, remesh and render
+              together, not the mesher alone);
+  downstream  device scene build, quad -> vertex expansion and the erosion
+              pyramid, with their rooflines;
+  cpu_baseline the CPU oracle on the same frame (all host cores, and one).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
