@@ -108,6 +108,10 @@ struct SrvRequest {
 struct Slot {
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
+  // edit batches: the render runs on stream2, forked after the edit and
+  // joined before the results are read, so it overlaps the remesh
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t forked = nullptr, joined = nullptr;
   meso_hit* d_hits = nullptr;
   uint64_t hit_cap = 0;  // pixels
   void* d_table = nullptr;
@@ -172,6 +176,9 @@ void release_slot(Slot& s) {
   cudaFreeHost(s.h_coords);
   cudaFreeHost(s.h_hits);
   if (s.done) cudaEventDestroy(s.done);
+  if (s.forked) cudaEventDestroy(s.forked);
+  if (s.joined) cudaEventDestroy(s.joined);
+  if (s.stream2) cudaStreamDestroy(s.stream2);
   if (s.stream) cudaStreamDestroy(s.stream);
   s = Slot();
 }
@@ -260,6 +267,10 @@ void launch_batch(meso_server* srv, Slot& s) {
     uint32_t n_dirty = 0;
     rc = edit_spheres(ctx, scene, r.edits.data(), (uint32_t)r.edits.size(), srv->dirty.data(),
                       (uint32_t)srv->dirty.size(), &n_dirty, st);
+    if (rc == MESO_OK) {
+      cudaEventRecord(s.forked, st);
+      cudaStreamWaitEvent(s.stream2, s.forked, 0);
+    }
     if (rc == MESO_OK && n_dirty > s.coord_cap) rc = fail(MESO_ERR_OVERFLOW, "server: too many dirty chunks");
     if (rc == MESO_OK && n_dirty) {
       const int CX = scene->nx / 32, CY = scene->ny / 32;
@@ -285,13 +296,18 @@ void launch_batch(meso_server* srv, Slot& s) {
     }
     s.n_dirty = n_dirty;
   }
+  const cudaStream_t rs = s.edit ? s.stream2 : st;  // the render's stream
   if (rc == MESO_OK)
     rc = launch_raymarch(ctx, scenes.data(), cams.data(), (uint32_t)cams.size(), srv->light, s.reqs[0].req.flags,
-                         s.d_hits, st, s.d_table, s.table_bytes);
+                         s.d_hits, rs, s.d_table, s.table_bytes);
   if (rc == MESO_OK) {
     dim3 grid(64, segs.n);
-    hit_hash_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<const uint64_t*>(s.d_hits), segs, s.d_sums);
+    hit_hash_kernel<<<grid, 256, 0, rs>>>(reinterpret_cast<const uint64_t*>(s.d_hits), segs, s.d_sums);
     ctx->launches.fetch_add(s.edit ? 2 : 1);
+    if (s.edit) {
+      cudaEventRecord(s.joined, rs);
+      cudaStreamWaitEvent(st, s.joined, 0);
+    }
     cudaMemcpyAsync(s.h_sums, s.d_sums, sizeof(unsigned long long) * (2 * kMaxBatch + 2), cudaMemcpyDeviceToHost, st);
     if (srv->cfg.keep_hits) cudaMemcpyAsync(s.h_hits, s.d_hits, off * sizeof(meso_hit), cudaMemcpyDeviceToHost, st);
   }
@@ -429,7 +445,10 @@ meso_status meso_server_create(meso_ctx* ctx, const meso_server_config* cfg, mes
   srv->slots.resize(n_slots);
   for (auto& s : srv->slots) {
     cudaError_t e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s.stream2, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.forked, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.joined, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&s.d_hits, srv->cfg.max_batch_rays * sizeof(meso_hit));
     s.hit_cap = srv->cfg.max_batch_rays;
     s.table_bytes = raymarch_view_table_bytes(kMaxBatch);
