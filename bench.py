@@ -264,6 +264,65 @@ def bench_mesh(ctx, meso, steps, warmup):
             "gvox_s_plain": vox / (ms_plain * 1e6), "algo_bytes": algo, "data": data, "qbuf": qbuf}
 
 
+def bench_mesh_u8(ctx, meso, m, steps):
+    """The 8-bit sources: the same 4096 chunks with materials folded into
+    1..255 (three persistent CTAs per SM fit, the staged chunk being 32 KiB),
+    and the small dense case, a 256^3 uint8 grid meshed as 512 chunks with
+    their neighbours' faces, batched and one launch per chunk."""
+    import ctypes
+    L = meso._lib
+    h = m["data"].download(np.uint16)
+    data = ctx.to_device(np.where(h > 0, 1 + (h.astype(np.uint32) % 255), 0).astype(np.uint8))
+    del h
+    cnt = ctx.alloc(8)
+    flush = ctx.alloc(L2_FLUSH_BYTES)
+    total = ctypes.c_uint64()
+
+    def timed(src, coords, n, per_launch=False, reps=steps):
+        out = meso.MeshOutput(m["qbuf"].ptr, MESH_CHUNKS * 8192, cnt.ptr, None)
+        fn = L.meso_mesh_chunks_per_launch if per_launch else L.meso_mesh_chunks
+        cp = coords.ptr if coords is not None else None
+        for _ in range(3):
+            meso._check(fn(ctx.handle, ctypes.byref(src), cp, n, ctypes.byref(out), None))
+        evs = [(ctx.event(), ctx.event()) for _ in range(reps)]
+        for a, b in evs:
+            flush.zero()
+            ctx.record(a)
+            meso._check(fn(ctx.handle, ctypes.byref(src), cp, n, ctypes.byref(out), None))
+            ctx.record(b)
+        ctx.sync()
+        meso._check(L.meso_mesh_check(ctx.handle, ctypes.byref(out), None, ctypes.byref(total)))
+        return sum(ctx.elapsed_ms(a, b) for a, b in evs) / reps, int(total.value)
+
+    src = meso.MeshSource()
+    src.kind = meso.SRC_CHUNKS_U8
+    src.d_data = data.ptr
+    ms, quads = timed(src, None, MESH_CHUNKS)
+    hbm = peaks()[0]
+    algo = MESH_CHUNKS * 32768 + 8 * quads
+    ach = algo / (ms * 1e6)
+    res = {"workload": f"the {MESH_CHUNKS} chunks as uint8 (materials folded into 1..255)",
+           "gvox_s": round(MESH_CHUNKS * 32768 / (ms * 1e6), 2), "ms": round(ms, 4), "quads": quads,
+           "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+                        "frac": round(ach / hbm, 4), "algorithmic_bytes_per_launch": algo,
+                        "kernel": "mesh_kernel<CHUNKS_U8>"}}
+    del data
+    g = ctx.generate_dense_u8(256, 256, 256, seed=1)
+    coords = ctx.to_device(np.array([(x, y, z) for z in range(8) for y in range(8) for x in range(8)], np.int32))
+    gs = meso.MeshSource()
+    gs.kind = meso.SRC_GRID_U8
+    gs.d_data = g.ptr
+    gs.nx = gs.ny = gs.nz = 256
+    ms_b, q_b = timed(gs, coords, 512)
+    ms_p, q_p = timed(gs, coords, 512, per_launch=True, reps=max(1, min(steps, 3)))
+    assert q_b == q_p
+    res["dense_256"] = {"workload": "256^3 uint8 value-noise grid (3 octaves, seed 1), 512 chunks with neighbour faces",
+                        "gvox_s": round(512 * 32768 / (ms_b * 1e6), 2), "ms": round(ms_b, 4), "quads": q_b,
+                        "per_chunk_launch_gvox_s": round(512 * 32768 / (ms_p * 1e6), 3),
+                        "batched_over_per_launch": round(ms_p / ms_b, 2)}
+    return res
+
+
 def cpu_mesh_baseline(m, n_single=512):
     """Oracle mesher on the host cores: all threads over the whole batched
     workload (checked bit for bit against the GPU's quads), one thread over
@@ -621,6 +680,7 @@ def run_ours(args, world, rank, local, dist):
         }
         if not args.skip_cpu:
             line["mesh"]["cpu_baseline"] = cpu_mesh_baseline(m)
+        line["mesh"]["uint8"] = bench_mesh_u8(ctx, meso, m, args.steps)
         line["downstream"] = bench_downstream(ctx, meso, m, args.steps)
     if rank == 0 and not args.skip_serve:
         line["served"] = bench_serve_render(ctx, meso, args.serve_seconds)

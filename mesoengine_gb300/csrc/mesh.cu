@@ -8,8 +8,9 @@
 // (Runtimes/Voxel/Chunk/ChunkManager.h:183-210).  Here a persistent kernel
 // pulls chunks from a device ticket queue and emits greedy quads.
 //
-// Two CTAs of 8 warps share each SM, each meshing its own chunk, so one
-// CTA's barrier-separated phases overlap the other's work.  Per chunk:
+// Two CTAs of 8 warps share each SM (three for 8-bit sources, whose staged
+// chunk is half the size), each meshing its own chunk, so one CTA's
+// barrier-separated phases overlap the others' work.  Per chunk:
 //  1. staging: the 32^3 materials arrive in shared memory through TMA (one
 //     bulk copy per chunk of a chunk array, one 3-D tensor box per chunk of a
 //     dense grid, one 1 KiB bulk copy per occupied brick of a brick map); the
@@ -48,12 +49,12 @@ constexpr int kS = 33;               // padded row stride of 32x32 word arrays
 constexpr int kArr = 32 * kS;
 constexpr int kQBuf = 128;           // staged quads per warp
 constexpr int kBrickSlot = 1040;     // bytes per staged brick (bank-spread padding)
-constexpr int kMatBuf = 64 * kBrickSlot;
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 
+// Shared memory of one CTA: these arrays, then the staged materials of the
+// chunk (KindTraits::kMatBytes, 128-byte aligned).
 struct __align__(128) MeshSmem {
-  uint8_t mat[kMatBuf];
   uint32_t occ[kArr];                     // occupancy, bits over x, [z][y]
   uint32_t occt[kArr];                    // occupancy, bits over y, [z][x]
   uint32_t ex[kArr], ey[kArr], ez[kArr];  // equality with -x / -y / -z neighbour, bits over x, [z][y]
@@ -69,7 +70,6 @@ struct __align__(128) MeshSmem {
   uint32_t task_next;                     // dynamic task counter of the greedy
   uint32_t any_solid;
 };
-static_assert(sizeof(MeshSmem) + 128 <= 113 * 1024, "two mesher CTAs must fit in one SM");
 
 struct MeshParams {
   const uint8_t* data;
@@ -91,33 +91,32 @@ struct MeshParams {
   int32_t use_queue;
 };
 
+// Per source kind: halo reads, addressing, element size, the staged bytes of
+// one chunk, and the CTAs that fit one SM (228 KB of shared memory, 1 KB of
+// it reserved per CTA): 8-bit chunks stage 32 KiB, so three CTAs fit.
 template <int KIND>
 struct KindTraits;
-template <>
-struct KindTraits<MESO_SRC_CHUNKS_U16> {
-  static constexpr bool kHalo = false, kGrid = false, kBrick = false;
-  static constexpr int kElem = 2;
+template <int KIND>
+struct KindBase {
+  static constexpr bool kHalo = KIND != MESO_SRC_CHUNKS_U16 && KIND != MESO_SRC_CHUNKS_U8;
+  static constexpr bool kGrid = KIND == MESO_SRC_GRID_U8 || KIND == MESO_SRC_GRID_U16;
+  static constexpr bool kBrick = KIND == MESO_SRC_BRICKMAP;
+  static constexpr int kElem = KIND == MESO_SRC_CHUNKS_U8 || KIND == MESO_SRC_GRID_U8 ? 1 : 2;
+  static constexpr int kMatBytes = kBrick ? 64 * kBrickSlot : 32768 * kElem;
+  static constexpr int kCtasPerSm = kElem == 1 ? 3 : 2;
+  static_assert(sizeof(MeshSmem) + kMatBytes + 128 + 1024 <= 228 * 1024 / kCtasPerSm,
+                "the mesher's CTAs per SM must fit the shared memory");
 };
 template <>
-struct KindTraits<MESO_SRC_CHUNKS_U8> {
-  static constexpr bool kHalo = false, kGrid = false, kBrick = false;
-  static constexpr int kElem = 1;
-};
+struct KindTraits<MESO_SRC_CHUNKS_U16> : KindBase<MESO_SRC_CHUNKS_U16> {};
 template <>
-struct KindTraits<MESO_SRC_GRID_U8> {
-  static constexpr bool kHalo = true, kGrid = true, kBrick = false;
-  static constexpr int kElem = 1;
-};
+struct KindTraits<MESO_SRC_CHUNKS_U8> : KindBase<MESO_SRC_CHUNKS_U8> {};
 template <>
-struct KindTraits<MESO_SRC_GRID_U16> {
-  static constexpr bool kHalo = true, kGrid = true, kBrick = false;
-  static constexpr int kElem = 2;
-};
+struct KindTraits<MESO_SRC_GRID_U8> : KindBase<MESO_SRC_GRID_U8> {};
 template <>
-struct KindTraits<MESO_SRC_BRICKMAP> {
-  static constexpr bool kHalo = true, kGrid = false, kBrick = true;
-  static constexpr int kElem = 2;
-};
+struct KindTraits<MESO_SRC_GRID_U16> : KindBase<MESO_SRC_GRID_U16> {};
+template <>
+struct KindTraits<MESO_SRC_BRICKMAP> : KindBase<MESO_SRC_BRICKMAP> {};
 
 template <int KIND>
 __device__ __forceinline__ uint32_t load_mat(const uint8_t* buf, int x, int y, int z) {
@@ -190,7 +189,8 @@ __device__ __forceinline__ uint32_t global_solid(const MeshParams& p, int gx, in
 // the next ticket, requested one ticket ahead so the atomic's latency is
 // hidden behind a chunk's work.
 template <int KIND>
-__device__ __forceinline__ void issue_chunk(MeshSmem& sm, const MeshParams& p, const CUtensorMap* tmap, int lane,
+__device__ __forceinline__ void issue_chunk(MeshSmem& sm, uint8_t* dst, const MeshParams& p, const CUtensorMap* tmap,
+                                            int lane,
                                             uint32_t& cur, uint32_t& end, uint32_t& pending) {
   using T = KindTraits<KIND>;
   int c = -1;
@@ -213,7 +213,6 @@ __device__ __forceinline__ void issue_chunk(MeshSmem& sm, const MeshParams& p, c
   if (lane == 0) sm.chunk = c;
   if (c < 0) return;
   uint64_t* bar = &sm.bar;
-  uint8_t* dst = sm.mat;
   if constexpr (!T::kGrid && !T::kBrick) {
     if (lane == 0) {
       // with an index list, p.nx is the number of chunks in the array
@@ -444,13 +443,14 @@ __device__ __forceinline__ void flush_warp(MeshSmem& sm, int warp, const MeshPar
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, KindTraits<KIND>::kCtasPerSm)
     mesh_kernel(const MeshParams p, const __grid_constant__ CUtensorMap tmap) {
   using T = KindTraits<KIND>;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t base_addr = smem_u32(smem_raw);
   const uint32_t pad = (128u - (base_addr & 127u)) & 127u;
   MeshSmem& sm = *reinterpret_cast<MeshSmem*>(smem_raw + pad);
+  uint8_t* const mat = smem_raw + pad + sizeof(MeshSmem);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   uint32_t cur = p.use_queue ? 0u : blockIdx.x, end = 0, pending = 0;
@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   uint32_t phase = 0;
   uint32_t qc = 0;  // quads staged in qbuf[warp] (warp-uniform)
   for (;;) {
-    if (warp == 0) issue_chunk<KIND>(sm, p, &tmap, lane, cur, end, pending);
+    if (warp == 0) issue_chunk<KIND>(sm, mat, p, &tmap, lane, cur, end, pending);
     __syncthreads();
     const int c = sm.chunk;
     if (c < 0) break;
@@ -491,7 +491,7 @@ __global__ void __launch_bounds__(kThreads, 2)
       return;
     }
     if (valid) {
-      const uint8_t* mb = sm.mat;
+      const uint8_t* mb = mat;
       // ---- pass 1: warp w builds slabs z0 .. z0+3 (z0 = 4w; lanes = x),
       // 8 rows of the 4 slabs at a time, so the previous slab's materials
       // are still in registers for the -z equality.  Row words come from
@@ -849,7 +849,7 @@ meso_status make_grid_map(const meso_mesh_source* src, int elem, CUtensorMap* ma
 template <int KIND>
 meso_status launch_kind(meso_ctx* ctx, const MeshParams& base, const CUtensorMap& tmap, uint32_t n_chunks,
                         cudaStream_t st, bool per_launch) {
-  const size_t smem = sizeof(MeshSmem) + 128;
+  const size_t smem = sizeof(MeshSmem) + KindTraits<KIND>::kMatBytes + 128;
   static bool attr_set[64] = {false};
   if (!attr_set[ctx->device & 63]) {
     MESO_CUDA_TRY(cudaFuncSetAttribute(mesh_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -876,7 +876,10 @@ meso_status launch_kind(meso_ctx* ctx, const MeshParams& base, const CUtensorMap
   }
   MeshParams p = base;
   p.use_queue = 1;
-  uint32_t grid = ctx->sm_count * (ctx->tuning.mesh_ctas_per_sm ? ctx->tuning.mesh_ctas_per_sm : 2);
+  // CTAs per SM: the tuned value, at most (and by default) what fits the SM
+  constexpr uint32_t kMaxCtas = KindTraits<KIND>::kCtasPerSm;
+  const uint32_t tuned = ctx->tuning.mesh_ctas_per_sm;
+  uint32_t grid = ctx->sm_count * (tuned && tuned < kMaxCtas ? tuned : kMaxCtas);
   const uint32_t per = p.per_ticket ? p.per_ticket : 1;
   const uint32_t need = (n_chunks + per - 1) / per;
   if (grid > need) grid = need;
@@ -953,6 +956,5 @@ meso_status launch_mesh(meso_ctx* ctx, const meso_mesh_source* src, const int32_
   }
 }
 
-size_t mesh_smem_bytes() { return sizeof(MeshSmem) + 128; }
 
 }  // namespace meso

@@ -78,6 +78,30 @@ def test_component_patterns_match_oracle(ctx):
     assert np.array_equal(_sorted(q8), oracle.mesh_chunks(oracle.SRC_CHUNKS_U8, c8))
 
 
+def test_ctas_per_sm_settings_agree():
+    # 8-bit sources run up to three persistent CTAs per SM, 16-bit ones two;
+    # every setting (larger ones are capped) gives the same quads
+    c16 = _component_chunks()[:8]
+    c8 = np.where(c16 > 0, 1 + (c16.astype(np.uint32) % 255), 0).astype(np.uint8)
+    ref16 = oracle.mesh_chunks(oracle.SRC_CHUNKS_U16, c16)
+    ref8 = oracle.mesh_chunks(oracle.SRC_CHUNKS_U8, c8)
+    for cps in (1, 2, 3):
+        cx = meso.Context(0, mesh_ctas_per_sm=cps)
+        try:
+            d16, d8 = cx.to_device(c16), cx.to_device(c8)
+            q16, _ = cx.mesh(meso.SRC_CHUNKS_U16, d16, n=c16.shape[0])
+            q8, _ = cx.mesh(meso.SRC_CHUNKS_U8, d8, n=c8.shape[0])
+            d16.free()
+            d8.free()
+            assert np.array_equal(_sorted(q16), ref16)
+            assert np.array_equal(_sorted(q8), ref8)
+        finally:
+            cx.close()
+    with pytest.raises(meso.MesoError) as e:
+        meso.Context(0, mesh_ctas_per_sm=4)
+    assert e.value.status == 1
+
+
 def test_generated_chunks_match_oracle(ctx):
     n = 48
     dev, solid = ctx.generate_chunks_u16(n, seed0=1)
