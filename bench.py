@@ -266,8 +266,7 @@ def bench_mesh(ctx, meso, steps, warmup):
 
 def bench_mesh_u8(ctx, meso, m, steps):
     """The 8-bit sources: the same 4096 chunks with materials folded into
-    1..255 (three persistent CTAs per SM fit, the staged chunk being 32 KiB),
-    and the small dense case, a 256^3 uint8 grid meshed as 512 chunks with
+    1..255, and the small dense case, a 256^3 uint8 grid meshed as 512 chunks with
     their neighbours' faces, batched and one launch per chunk."""
     import ctypes
     L = meso._lib

@@ -55,9 +55,8 @@ typedef struct meso_config {
   uint32_t chunk_edge;            /* must be 32 (or 0) */
   uint32_t brick_edge;            /* must be 8 (or 0) */
   int32_t device;                 /* CUDA device ordinal */
-  uint32_t mesh_ctas_per_sm;      /* persistent mesher CTAs per SM, 1..3 (0 = tuned/default: as many as
-                                     fit, 3 for 8-bit sources, 2 for 16-bit ones; larger values are
-                                     capped at that) */
+  uint32_t mesh_ctas_per_sm;      /* persistent mesher CTAs (16 warps each) per SM, 1..2
+                                     (0 = tuned/default 2) */
   uint32_t mesh_chunks_per_ticket;/* chunks taken per queue ticket (0 = tuned/default 1) */
   uint32_t ray_tile_w, ray_tile_h;/* threads of one ray CTA tile (0 = tuned/default 8x4 per warp) */
   uint32_t ray_warps_per_cta;     /* 1..4, 0 = tuned/default */

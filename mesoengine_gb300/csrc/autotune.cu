@@ -137,7 +137,7 @@ extern "C" meso_status meso_autotune(meso_ctx* ctx, const char* path) {
     ctx->tuning = saved;
     return rc;
   }
-  best.mesh_ctas_per_sm = 0;  // as many CTAs per SM as the source kind's shared memory allows
+  best.mesh_ctas_per_sm = 0;  // the default: two 16-warp CTAs per SM, what registers and shared memory allow
   ctx->tuning = best;
   if (path && *path) {
     FILE* f = fopen(path, "w");

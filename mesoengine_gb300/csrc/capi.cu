@@ -117,14 +117,13 @@ meso_status meso_ctx_create(const meso_config* cfg, meso_ctx** out) {
   ctx->sm_count = prop.multiProcessorCount;
   load_tuning(c.tuning_path, ctx->tuning);
   if (ctx->tuning.ray_warps_per_cta > 4) ctx->tuning.ray_warps_per_cta = 4;  // files from older tunings
-  // 0 = as many mesher CTAs per SM as fit: 3 for 8-bit sources, 2 for 16-bit ones
-  if (ctx->tuning.mesh_ctas_per_sm > 3) ctx->tuning.mesh_ctas_per_sm = 0;
+  if (ctx->tuning.mesh_ctas_per_sm > 2) ctx->tuning.mesh_ctas_per_sm = 0;  // 0: two CTAs per SM
   if (c.mesh_ctas_per_sm) ctx->tuning.mesh_ctas_per_sm = c.mesh_ctas_per_sm;
   if (c.mesh_chunks_per_ticket) ctx->tuning.mesh_chunks_per_ticket = c.mesh_chunks_per_ticket;
   if (c.ray_tile_w) ctx->tuning.ray_tile_w = c.ray_tile_w;
   if (c.ray_warps_per_cta) ctx->tuning.ray_warps_per_cta = c.ray_warps_per_cta;
   if (32 % ctx->tuning.ray_tile_w || ctx->tuning.ray_warps_per_cta == 0 || ctx->tuning.ray_warps_per_cta > 4 ||
-      ctx->tuning.mesh_ctas_per_sm > 3) {
+      ctx->tuning.mesh_ctas_per_sm > 2) {
     delete ctx;
     return fail(MESO_ERR_INVALID_ARG, "ctx_create: bad ray tile or mesher configuration");
   }

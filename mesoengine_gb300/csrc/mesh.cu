@@ -8,9 +8,10 @@
 // (Runtimes/Voxel/Chunk/ChunkManager.h:183-210).  Here a persistent kernel
 // pulls chunks from a device ticket queue and emits greedy quads.
 //
-// Two CTAs of 8 warps share each SM (three for 8-bit sources, whose staged
-// chunk is half the size), each meshing its own chunk, so one CTA's
-// barrier-separated phases overlap the others' work.  Per chunk:
+// Two CTAs of 16 warps share each SM (64 registers per thread), each meshing
+// its own chunk, so one CTA's barrier-separated phases overlap the other's
+// work; the kernel is latency bound and 32 resident warps hide more of it
+// than 16 or 24 did.  Per chunk:
 //  1. staging: the 32^3 materials arrive in shared memory through TMA (one
 //     bulk copy per chunk of a chunk array, one 3-D tensor box per chunk of a
 //     dense grid, one 1 KiB bulk copy per occupied brick of a brick map); the
@@ -28,7 +29,7 @@
 //     scanned with run-length bit tricks (Lysenko's order: first unconsumed
 //     face, widen along u while the material matches, grow along v while the
 //     whole run matches); quads are staged per warp in shared memory and
-//     appended to global memory with one atomic per 128 quads.
+//     appended to global memory with one atomic per 64 quads.
 #include <cudaTypedefs.h>
 
 #include <cstdio>
@@ -41,13 +42,16 @@ namespace {
 
 using namespace ::meso::dev;
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
-constexpr int kGroups = 192 / kWarps;  // word groups (direction, row) per warp: 4 rows x 6 directions
-static_assert(kWarps * 4 == 32, "the isolated-face pass gives each warp 4 rows");
+// Warps w and w + 8 form a pair that shares rows (and slabs) 4(w mod 8) ..
+// 4(w mod 8) + 3: in the mask pass each builds half of the slabs' rows, in
+// the isolated-face passes each takes three of the six face directions.
+constexpr int kGroups = 12;  // word groups (direction, row) per warp: 4 rows x 3 directions
+static_assert(kWarps == 16, "eight warp pairs of 4 rows each");
 constexpr int kS = 33;               // padded row stride of 32x32 word arrays
 constexpr int kArr = 32 * kS;
-constexpr int kQBuf = 128;           // staged quads per warp
+constexpr int kQBuf = 64;            // staged quads per warp
 constexpr int kBrickSlot = 1040;     // bytes per staged brick (bank-spread padding)
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
@@ -92,8 +96,8 @@ struct MeshParams {
 };
 
 // Per source kind: halo reads, addressing, element size, the staged bytes of
-// one chunk, and the CTAs that fit one SM (228 KB of shared memory, 1 KB of
-// it reserved per CTA): 8-bit chunks stage 32 KiB, so three CTAs fit.
+// one chunk, and the CTAs per SM (two of 16 warps: the register file allows
+// no more, and 16-bit chunks fill the shared memory of two).
 template <int KIND>
 struct KindTraits;
 template <int KIND>
@@ -103,7 +107,7 @@ struct KindBase {
   static constexpr bool kBrick = KIND == MESO_SRC_BRICKMAP;
   static constexpr int kElem = KIND == MESO_SRC_CHUNKS_U8 || KIND == MESO_SRC_GRID_U8 ? 1 : 2;
   static constexpr int kMatBytes = kBrick ? 64 * kBrickSlot : 32768 * kElem;
-  static constexpr int kCtasPerSm = kElem == 1 ? 3 : 2;
+  static constexpr int kCtasPerSm = 2;
   static_assert(sizeof(MeshSmem) + kMatBytes + 128 + 1024 <= 228 * 1024 / kCtasPerSm,
                 "the mesher's CTAs per SM must fit the shared memory");
 };
@@ -442,6 +446,42 @@ __device__ __forceinline__ void flush_warp(MeshSmem& sm, int warp, const MeshPar
   __syncwarp();
 }
 
+// Barrier of the warp pair that shares row group g (ids 1..8; 0 is __syncthreads).
+__device__ __forceinline__ void pair_sync(int g) {
+  asm volatile("bar.sync %0, 64;" ::"r"(1 + g) : "memory");
+}
+
+// Isolated faces of the three directions DB .. DB+2 for the rows v0 .. v0+3
+// (lane = slice); see pass 2 in the kernel.
+template <int DB>
+__device__ __forceinline__ void isolated_rows(MeshSmem& sm, int v0, int lane, uint32_t (&isow)[kGroups],
+                                              uint32_t& lane_iso) {
+#pragma unroll
+  for (int dd = 0; dd < 3; dd++) {
+    const int d = DB + dd;
+    uint32_t fu = v0 > 0 ? face_row(sm, d, v0 - 1, lane) : 0u;
+    uint32_t fv = face_row(sm, d, v0, lane);
+    uint32_t vv = v_arr(sm, d)[word_off(d, lane, v0)];
+    uint32_t rest = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int v = v0 + q;
+      const bool last = q == 3 && v0 == 28;
+      const uint32_t fd = last ? 0u : face_row(sm, d, v + 1, lane);
+      const uint32_t vd = last ? 0u : v_arr(sm, d)[word_off(d, lane, v + 1)];
+      const uint32_t w = isolated(fv, fu, fd, e_arr(sm, d)[word_off(d, lane, v)], vv, vd);
+      isow[4 * dd + q] = w;
+      lane_iso += __popc(w);
+      rest |= fv & ~w;
+      fu = fv;
+      fv = fd;
+      vv = vd;
+    }
+    const uint32_t m = __ballot_sync(kFull, rest != 0u);
+    if (lane == 0 && m) atomicOr(&sm.rest_slices[d], m);
+  }
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(kThreads, KindTraits<KIND>::kCtasPerSm)
     mesh_kernel(const MeshParams p, const __grid_constant__ CUtensorMap tmap) {
@@ -492,16 +532,20 @@ __global__ void __launch_bounds__(kThreads, KindTraits<KIND>::kCtasPerSm)
     }
     if (valid) {
       const uint8_t* mb = mat;
-      // ---- pass 1: warp w builds slabs z0 .. z0+3 (z0 = 4w; lanes = x),
-      // 8 rows of the 4 slabs at a time, so the previous slab's materials
-      // are still in registers for the -z equality.  Row words come from
-      // ballots and are stored by lane 0; the transposed copies for the X
-      // faces are made at the end.
+      // ---- pass 1: the warp pair of row group g builds slabs z0 .. z0+3
+      // (z0 = 4g; lanes = x), warp w < 8 rows 0..15 and warp w + 8 rows
+      // 16..31, 8 rows of the 4 slabs at a time, so the previous slab's
+      // materials are still in registers for the -z equality.  Row words come
+      // from ballots and are stored by lane 0; after a pair barrier each warp
+      // makes the transposed copies (for the X faces) of two of the slabs.
       {
-        const int z0 = warp * 4;
-        uint32_t prev_m[4] = {0, 0, 0, 0};  // row y0-1 of each slab
+        const int g = warp & 7, half = warp >> 3;
+        const int z0 = g * 4, ybeg = half * 16;
+        uint32_t prev_m[4];  // row y0-1 of each slab
+#pragma unroll
+        for (int j = 0; j < 4; j++) prev_m[j] = half ? load_mat<KIND>(mb, lane, ybeg - 1, z0 + j) : 0u;
 #pragma unroll 1
-        for (int y0 = 0; y0 < 32; y0 += 8) {
+        for (int y0 = ybeg; y0 < ybeg + 16; y0 += 8) {
           uint32_t mp[8];  // rows y0 .. y0+7 of the slab below
 #pragma unroll
           for (int k = 0; k < 8; k++) mp[k] = z0 > 0 ? load_mat<KIND>(mb, lane, y0 + k, z0 - 1) : 0u;
@@ -542,9 +586,10 @@ __global__ void __launch_bounds__(kThreads, KindTraits<KIND>::kCtasPerSm)
             for (int k = 0; k < 8; k++) mp[k] = m[k];
           }
         }
-        __syncwarp();
+        // the pair's other warp builds the other half of these slabs' rows
+        pair_sync(g);
 #pragma unroll 1
-        for (int j = 0; j < 4; j++) {
+        for (int j = 2 * half; j < 2 * half + 2; j++) {
           const int o = (z0 + j) * kS + lane;
           const uint32_t r_occ = sm.occ[o];
           uint32_t occT = 0, eyT = 0, ezT = 0;
@@ -567,35 +612,15 @@ __global__ void __launch_bounds__(kThreads, KindTraits<KIND>::kCtasPerSm)
         // the plane).  Quads never leave a component of same-material,
         // edge-adjacent faces, so these are 1x1 quads whatever the greedy
         // does elsewhere: they are peeled off into registers.  Warp w holds
-        // rows v0 .. v0+3 (v0 = 4w) of every direction (lane = slice),
-        // walking the rows in order so the face words of the rows above and
-        // below are carried, not recomputed.
-        const int v0 = warp * 4;
+        // rows v0 .. v0+3 (v0 = 4 (w mod 8)) of three directions (0-2 for
+        // w < 8, 3-5 for the others; lane = slice), walking the rows in order
+        // so the face words of the rows above and below are carried, not
+        // recomputed.
+        const int v0 = (warp & 7) * 4, dbase = (warp >> 3) * 3;
         uint32_t isow[kGroups];
         uint32_t lane_iso = 0;
-#pragma unroll
-        for (int d = 0; d < 6; d++) {
-          uint32_t fu = v0 > 0 ? face_row(sm, d, v0 - 1, lane) : 0u;
-          uint32_t fv = face_row(sm, d, v0, lane);
-          uint32_t vv = v_arr(sm, d)[word_off(d, lane, v0)];
-          uint32_t rest = 0;
-#pragma unroll
-          for (int q = 0; q < 4; q++) {
-            const int v = v0 + q;
-            const bool last = q == 3 && v0 == 28;
-            const uint32_t fd = last ? 0u : face_row(sm, d, v + 1, lane);
-            const uint32_t vd = last ? 0u : v_arr(sm, d)[word_off(d, lane, v + 1)];
-            const uint32_t w = isolated(fv, fu, fd, e_arr(sm, d)[word_off(d, lane, v)], vv, vd);
-            isow[4 * d + q] = w;
-            lane_iso += __popc(w);
-            rest |= fv & ~w;
-            fu = fv;
-            fv = fd;
-            vv = vd;
-          }
-          const uint32_t m = __ballot_sync(kFull, rest != 0u);
-          if (lane == 0 && m) atomicOr(&sm.rest_slices[d], m);
-        }
+        if (dbase) isolated_rows<3>(sm, v0, lane, isow, lane_iso);
+        else isolated_rows<0>(sm, v0, lane, isow, lane_iso);
         const uint32_t total = __reduce_add_sync(kFull, lane_iso);
         unsigned long long run = 0;
         if (lane == 0 && total) run = atomicAdd(p.count, (unsigned long long)total);
@@ -614,7 +639,7 @@ __global__ void __launch_bounds__(kThreads, KindTraits<KIND>::kCtasPerSm)
         // prefixes, then the row from the owning lane's packed running
         // counts, then __fns inside that word.
 #pragma unroll 1
-        for (int dir = 0; dir < 6; dir++) {
+        for (int dir = dbase; dir < dbase + 3; dir++) {
           // this direction's words are isow[0..3]; the rest shift down by 4
           const uint32_t w0 = isow[0], w1 = isow[1], w2 = isow[2], w3 = isow[3];
 #pragma unroll

@@ -42,7 +42,7 @@ enum : uint32_t {
 };
 
 struct Tuning {
-  uint32_t mesh_ctas_per_sm = 0;  // 0: as many as fit (3 for 8-bit sources, 2 for 16-bit)
+  uint32_t mesh_ctas_per_sm = 0;  // 0: two 16-warp CTAs per SM
   uint32_t mesh_chunks_per_ticket = 1;
   uint32_t ray_tile_w = 8;  // lanes of one warp along x
   uint32_t ray_warps_per_cta = 4;
