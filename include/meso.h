@@ -84,6 +84,12 @@ int meso_sm_count(const meso_ctx* ctx);
  * flags the timeout and exits, and the call returns MESO_ERR_TIMEOUT; the
  * context stays usable. */
 meso_status meso_selftest_bounded_wait(meso_ctx* ctx, uint32_t limit_us);
+/* Measurement helper (no counterpart in the reference): the L2 read
+ * bandwidth, the denominator for work whose fetches hit in L2 (the
+ * raymarch's).  A device buffer of `bytes` (16 KiB .. 64 MiB, a multiple of
+ * 16, so it stays in L2) is read once untimed and then `passes` times
+ * (1..1000) with 16-byte loads that bypass L1; *gb_s = bytes * passes / time. */
+meso_status meso_measure_l2_read(meso_ctx* ctx, uint64_t bytes, uint32_t passes, double* gb_s);
 
 /* Device memory, streams and events for callers without another CUDA host
  * library (tests, the Python binding). */

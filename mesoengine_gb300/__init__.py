@@ -195,6 +195,7 @@ _SIGNATURES = {
     "meso_graph_launch": [ctypes.c_void_p, ctypes.c_void_p],
     "meso_graph_destroy": [ctypes.c_void_p],
     "meso_selftest_bounded_wait": [ctypes.c_void_p, ctypes.c_uint32],
+    "meso_measure_l2_read": [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(ctypes.c_double)],
     "meso_raymarch_noalloc": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Camera),
                               ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p],
 }
@@ -600,6 +601,12 @@ class Context:
         """Runs a device wait that must give up after limit_us; raises
         MesoError(MESO_ERR_TIMEOUT) when the failure path works."""
         _check(_lib.meso_selftest_bounded_wait(self.handle, limit_us))
+
+    def measure_l2_read(self, nbytes: int = 32 << 20, passes: int = 50) -> float:
+        """L2 read bandwidth in GB/s (an L2-resident buffer read `passes` times)."""
+        g = ctypes.c_double()
+        _check(_lib.meso_measure_l2_read(self.handle, nbytes, passes, ctypes.byref(g)))
+        return g.value
 
     def autotune(self, path: str | None = None) -> None:
         _check(_lib.meso_autotune(self.handle, path.encode() if path else None))

@@ -76,6 +76,21 @@ __global__ void bounded_wait_probe_kernel(uint64_t limit_ns, uint32_t* err) {
   const bool ok = meso::dev::mbar_wait_bounded(&bar, 0, limit_ns);
   if (!ok && threadIdx.x == 0) atomicOr(err, meso::ERR_TIMEOUT);
 }
+
+// Reads an L2-resident buffer `passes` times with 16-byte cache-global loads
+// (L1 bypassed); the XOR of every word keeps the loads from being dropped.
+__global__ void l2_read_kernel(const uint4* __restrict__ buf, size_t n16, uint32_t passes, uint32_t* sink) {
+  uint32_t acc = 0;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (uint32_t k = 0; k < passes; k++) {
+#pragma unroll 4
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) {
+      const uint4 v = __ldcg(buf + i);
+      acc ^= v.x ^ v.y ^ v.z ^ v.w;
+    }
+  }
+  if (acc == 0x9E3779B9u) atomicAdd(sink, 1u);
+}
 }  // namespace
 
 extern "C" {
@@ -176,6 +191,37 @@ meso_status meso_selftest_bounded_wait(meso_ctx* ctx, uint32_t limit_us) {
   ctx->launches.fetch_add(1);
   MESO_CUDA_TRY(cudaGetLastError());
   return meso_sync(ctx, nullptr);
+}
+
+meso_status meso_measure_l2_read(meso_ctx* ctx, uint64_t bytes, uint32_t passes, double* gb_s) {
+  if (!ctx || !gb_s || bytes < (16u << 10) || bytes > (64u << 20) || bytes % 16 || passes == 0 || passes > 1000)
+    return fail(MESO_ERR_INVALID_ARG, "measure_l2_read: bytes must be 16 KiB .. 64 MiB (multiple of 16), passes 1..1000");
+  *gb_s = 0.0;
+  const cudaStream_t st = ctx->stream;
+  uint4* buf = nullptr;
+  MESO_CUDA_TRY(cudaMallocAsync(&buf, bytes, st));
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaMemsetAsync(buf, 0x5A, bytes, st);
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  const dim3 grid(ctx->sm_count * 8), block(256);
+  if (e == cudaSuccess) {
+    l2_read_kernel<<<grid, block, 0, st>>>(buf, bytes / 16, 1, ctx->d_scratch + 2);  // brings the buffer into L2
+    cudaEventRecord(a, st);
+    l2_read_kernel<<<grid, block, 0, st>>>(buf, bytes / 16, passes, ctx->d_scratch + 2);
+    cudaEventRecord(b, st);
+    ctx->launches.fetch_add(2);
+    e = cudaGetLastError();
+  }
+  float ms = 0.0f;
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  cudaFreeAsync(buf, st);
+  if (e != cudaSuccess) return cuda_fail(e, "measure_l2_read");
+  if (ms > 0.0f) *gb_s = (double)bytes * passes / (ms * 1e6);
+  return MESO_OK;
 }
 
 uint64_t meso_kernel_launches(const meso_ctx* ctx) { return ctx ? ctx->launches.load() : 0; }

@@ -59,7 +59,7 @@ struct meso_ctx {
   std::atomic<uint64_t> scene_bytes{0};
   std::atomic<uint64_t> launches{0};
   // small device scratch: [0] spare, [1] error flags, [2..63] spare
-  uint32_t* d_scratch = nullptr;
+  uint32_t* d_scratch = nullptr;  // 16 words: [1] device error flags, [2] sink of the L2 probe
   // ring of queue tickets for persistent mesh launches; consecutive launches
   // take consecutive counters, so up to kTicketRing launches may overlap on
   // different streams

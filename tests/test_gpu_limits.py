@@ -82,6 +82,16 @@ def test_downstream_limits(ctx):
     ctx.sync()
 
 
+def test_l2_read_measurement(ctx):
+    # the L2 probe reads an L2-resident buffer: faster than the HBM copy peak
+    g = ctx.measure_l2_read(32 << 20, 20)
+    assert g > 3000.0
+    L = meso.load()
+    out = ctypes.c_double()
+    for nbytes, passes in [(1 << 10, 10), ((64 << 20) + 16, 10), ((1 << 20) + 8, 10), (1 << 20, 0), (1 << 20, 1001)]:
+        assert L.meso_measure_l2_read(ctx.handle, nbytes, passes, ctypes.byref(out)) == INVALID_ARG
+
+
 def test_degenerate_workloads_match_oracle(ctx):
     # one solid voxel in the corner of a 32^3 scene; a 1x1 and a 1x7 image
     g = np.zeros((32, 32, 32), np.uint16)
