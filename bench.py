@@ -258,10 +258,31 @@ def bench_mesh(ctx, meso, steps, warmup):
     ms_plain = ctx.elapsed_ms(a, b)
     meso._check(L.meso_mesh_check(ctx.handle, ctypes.byref(out), None, ctypes.byref(total)))
     assert int(total.value) == quads
+    # the plain form captured once into a CUDA graph (4096 kernel nodes) and replayed
+    st = ctx.stream()
+
+    def plain_on_stream():
+        meso._check(L.meso_mesh_chunks_per_launch(ctx.handle, ctypes.byref(src), None, MESH_CHUNKS,
+                                                  ctypes.byref(out), st))
+
+    g = ctx.capture(plain_on_stream, st)
+    g.launch(st)
+    ctx.sync(st)
+    ga, gb = ctx.event(), ctx.event()
+    flush.zero(st)
+    ctx.record(ga, st)
+    g.launch(st)
+    ctx.record(gb, st)
+    ctx.sync(st)
+    ms_graph = ctx.elapsed_ms(ga, gb)
+    meso._check(L.meso_mesh_check(ctx.handle, ctypes.byref(out), st, ctypes.byref(total)))
+    assert int(total.value) == quads
+    g.destroy()
     vox = MESH_CHUNKS * 32768
     algo = MESH_CHUNKS * 65536 + 8 * quads
     return {"ms": ms, "ms_plain": ms_plain, "quads": quads, "gvox_s": vox / (ms * 1e6),
-            "gvox_s_plain": vox / (ms_plain * 1e6), "algo_bytes": algo, "data": data, "qbuf": qbuf}
+            "gvox_s_plain": vox / (ms_plain * 1e6), "gvox_s_graph": vox / (ms_graph * 1e6),
+            "algo_bytes": algo, "data": data, "qbuf": qbuf}
 
 
 def bench_mesh_u8(ctx, meso, m, steps):
@@ -675,6 +696,7 @@ def run_ours(args, world, rank, local, dist):
             "workload": f"{MESH_CHUNKS} standalone 32^3 uint16 chunks, occupancy log-uniform 0.1%-90%, 1-64 materials",
             "gvox_s": round(m["gvox_s"], 2), "ms": round(m["ms"], 4), "quads": m["quads"],
             "per_chunk_launch_gvox_s": round(m["gvox_s_plain"], 3),
+            "per_chunk_launch_graph_replay_gvox_s": round(m["gvox_s_graph"], 3),
             "batched_over_per_launch": round(m["ms_plain"] / m["ms"], 2),
             "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
                          "frac": round(ach / hbm, 4), "algorithmic_bytes_per_launch": m["algo_bytes"],
