@@ -68,7 +68,10 @@ typedef struct meso_ctx meso_ctx;
 typedef struct meso_scene meso_scene;
 
 /* Stands in for FChunkManage::Initialize (Runtimes/Voxel/Chunk/ChunkManager.h:90-102):
- * binds a device instead of spawning a host ThreadPool (Runtimes/Thread/ThreadPool.h:25-43). */
+ * binds a device instead of spawning a host ThreadPool (Runtimes/Thread/ThreadPool.h:25-43).
+ * Per-call temporaries come from the device's default stream-ordered memory
+ * pool; this raises that pool's release threshold (a per-process attribute)
+ * to at least 1 GiB so freed blocks are reused rather than remapped. */
 meso_status meso_ctx_create(const meso_config* cfg, meso_ctx** out);
 void meso_ctx_destroy(meso_ctx* ctx);
 const char* meso_last_error_string(void);

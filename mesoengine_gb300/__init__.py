@@ -352,7 +352,7 @@ class Scene:
         arr = (SphereEdit * max(1, len(spheres)))(*spheres)
         nx, ny, nz = self.dims
         cap = (nx // 32) * (ny // 32) * (nz // 32)
-        dirty = np.zeros(max(1, cap), dtype=np.uint32)
+        dirty = np.empty(max(1, cap), dtype=np.uint32)  # the library writes the first n entries
         n = ctypes.c_uint32()
         _check(_lib.meso_edit_spheres(self.ctx.handle, self.handle, arr, len(spheres), _np_ptr(dirty), cap,
                                       ctypes.byref(n), stream))

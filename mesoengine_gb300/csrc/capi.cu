@@ -150,7 +150,20 @@ meso_status meso_ctx_create(const meso_config* cfg, meso_ctx** out) {
   if (e == cudaSuccess) e = cudaMemset(ctx->d_scratch, 0, 64);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_tickets, 4 * meso_ctx::kTicketRing);
   if (e == cudaSuccess) e = cudaMemset(ctx->d_tickets, 0, 4 * meso_ctx::kTicketRing);
+  if (e == cudaSuccess) {
+    // per-call temporaries (edit lists, view tables, staging) come from the
+    // device's default stream-ordered pool; keeping up to 1 GiB of freed
+    // blocks cached there lets the next call reuse them instead of mapping
+    // fresh memory (which cost ~0.15 ms per sphere-edit call)
+    cudaMemPool_t pool = nullptr;
+    e = cudaDeviceGetDefaultMemPool(&pool, c.device);
+    uint64_t keep = 1ull << 30, cur = 0;
+    if (e == cudaSuccess) e = cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &cur);
+    if (e == cudaSuccess && cur < keep) e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   if (e != cudaSuccess) {
+    if (ctx->d_tickets) cudaFree(ctx->d_tickets);
+    if (ctx->d_scratch) cudaFree(ctx->d_scratch);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return cuda_fail(e, "ctx_create");

@@ -724,40 +724,66 @@ meso_status generate_chunks_u16(meso_ctx* ctx, uint32_t n, uint32_t seed0, uint1
 }
 
 // Host side of an edit: touched bricks (sorted unique) and dirty chunks.
+// Cells (bricks or chunks, edge `shift` bits of voxels) that the boxes
+// [lo, hi] of the spheres touch, as sorted unique linear indices of a grid
+// of G cells.  Small sets are collected and sorted; when the boxes cover a
+// sizeable part of the grid, a bitmap over the grid is marked and scanned
+// instead, so the cost stays bounded by the grid size.
+static void touched_cells(const int64_t (*lo)[3], const int64_t (*hi)[3], uint32_t n, int shift, const int64_t G[3],
+                          std::vector<uint32_t>& out) {
+  out.clear();
+  uint64_t volume = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    if (lo[i][0] > hi[i][0] || lo[i][1] > hi[i][1] || lo[i][2] > hi[i][2]) continue;
+    uint64_t v = 1;
+    for (int a = 0; a < 3; a++) v *= (uint64_t)((hi[i][a] >> shift) - (lo[i][a] >> shift) + 1);
+    volume += v;
+  }
+  const uint64_t total = (uint64_t)(G[0] * G[1] * G[2]);
+  const bool bitmap = volume > total / 64;
+  std::vector<uint64_t> bits;
+  if (bitmap) bits.assign((size_t)((total + 63) / 64), 0);
+  else out.reserve((size_t)volume);
+  for (uint32_t i = 0; i < n; i++) {
+    if (lo[i][0] > hi[i][0] || lo[i][1] > hi[i][1] || lo[i][2] > hi[i][2]) continue;
+    for (int64_t z = lo[i][2] >> shift; z <= hi[i][2] >> shift; z++)
+      for (int64_t y = lo[i][1] >> shift; y <= hi[i][1] >> shift; y++)
+        for (int64_t x = lo[i][0] >> shift; x <= hi[i][0] >> shift; x++) {
+          const uint64_t k = (uint64_t)(x + G[0] * (y + G[1] * z));
+          if (bitmap) bits[k >> 6] |= 1ull << (k & 63);
+          else out.push_back((uint32_t)k);
+        }
+  }
+  if (bitmap) {
+    for (size_t w = 0; w < bits.size(); w++)
+      for (uint64_t m = bits[w]; m; m &= m - 1) out.push_back((uint32_t)(w * 64 + (uint64_t)__builtin_ctzll(m)));
+  } else {
+    std::sort(out.begin(), out.end());
+    out.erase(std::unique(out.begin(), out.end()), out.end());
+  }
+}
+
+// The bricks a set of sphere edits may change (the voxel boxes of the
+// spheres) and the chunks to remesh (the boxes grown by one voxel, whose
+// faces may change), both sorted by linear index.
 static void edit_sets(const meso_scene* s, const meso_sphere_edit* sp, uint32_t n, std::vector<uint32_t>& bricks,
                       std::vector<uint32_t>& chunks) {
-  std::vector<uint8_t> cmark;
-  const int64_t CX = s->nx / 32, CY = s->ny / 32, CZ = s->nz / 32;
-  cmark.assign((size_t)(CX * CY * CZ), 0);
-  std::vector<uint32_t> b;
   const int64_t N[3] = {s->nx, s->ny, s->nz};
-  for (uint32_t i = 0; i < n; i++) {
-    int64_t lo[3], hi[3], clo[3], chi[3];
-    bool empty = false, cempty = false;
+  std::vector<int64_t> box((size_t)n * 12);
+  auto lo = reinterpret_cast<int64_t (*)[3]>(box.data());
+  auto hi = lo + n;
+  auto clo = hi + n;
+  auto chi = clo + n;
+  for (uint32_t i = 0; i < n; i++)
     for (int a = 0; a < 3; a++) {
-      lo[a] = std::max<int64_t>((int64_t)sp[i].center[a] - sp[i].radius, 0);
-      hi[a] = std::min<int64_t>((int64_t)sp[i].center[a] + sp[i].radius, N[a] - 1);
-      if (lo[a] > hi[a]) empty = true;
-      clo[a] = std::max<int64_t>((int64_t)sp[i].center[a] - sp[i].radius - 1, 0);
-      chi[a] = std::min<int64_t>((int64_t)sp[i].center[a] + sp[i].radius + 1, N[a] - 1);
-      if (clo[a] > chi[a]) cempty = true;
+      lo[i][a] = std::max<int64_t>((int64_t)sp[i].center[a] - sp[i].radius, 0);
+      hi[i][a] = std::min<int64_t>((int64_t)sp[i].center[a] + sp[i].radius, N[a] - 1);
+      clo[i][a] = std::max<int64_t>((int64_t)sp[i].center[a] - sp[i].radius - 1, 0);
+      chi[i][a] = std::min<int64_t>((int64_t)sp[i].center[a] + sp[i].radius + 1, N[a] - 1);
     }
-    if (!empty)
-      for (int64_t z = lo[2] >> 3; z <= hi[2] >> 3; z++)
-        for (int64_t y = lo[1] >> 3; y <= hi[1] >> 3; y++)
-          for (int64_t x = lo[0] >> 3; x <= hi[0] >> 3; x++)
-            b.push_back((uint32_t)(x + s->bx * (y + (int64_t)s->by * z)));
-    if (!cempty)
-      for (int64_t z = clo[2] >> 5; z <= chi[2] >> 5; z++)
-        for (int64_t y = clo[1] >> 5; y <= chi[1] >> 5; y++)
-          for (int64_t x = clo[0] >> 5; x <= chi[0] >> 5; x++) cmark[(size_t)(x + CX * (y + CY * z))] = 1;
-  }
-  std::sort(b.begin(), b.end());
-  b.erase(std::unique(b.begin(), b.end()), b.end());
-  bricks.swap(b);
-  chunks.clear();
-  for (size_t k = 0; k < cmark.size(); k++)
-    if (cmark[k]) chunks.push_back((uint32_t)k);
+  const int64_t B[3] = {s->bx, s->by, s->bz}, C[3] = {s->nx / 32, s->ny / 32, s->nz / 32};
+  touched_cells(lo, hi, n, 3, B, bricks);
+  touched_cells(clo, chi, n, 5, C, chunks);
 }
 
 meso_status edit_spheres(meso_ctx* ctx, meso_scene* s, const meso_sphere_edit* h_sp, uint32_t n, uint32_t* h_dirty,
