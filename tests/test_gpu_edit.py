@@ -91,3 +91,17 @@ def test_edit_remove_everything_unlinks_bricks(ctx):
     ptr = scene.download()[0]
     assert (ptr == meso.EMPTY_BRICK).all()
     assert scene.info().n_bricks == 0
+
+
+def test_large_edits_match_oracle(ctx):
+    # spheres whose boxes cover most of the grid take the bitmap path for the
+    # touched bricks and dirty chunks; small ones beside them the sorted path
+    t = meso.terrain_preset("small")
+    scene = ctx.scene_from_terrain(t, spare_bricks=1 << 16)
+    bm = oracle.HostBrickMap.from_terrain(_oracle_terrain(t))
+    dims = (t.nx, t.ny, t.nz)
+    for sp in ([([64, 64, 40], 90, 0)], [([20, 100, 10], 70, 513), ([5, 5, 5], 3, 9)], [([64, 64, 64], 200, 77)]):
+        dirty = scene.edit(_dev(sp))
+        bm.edit(_host(sp))
+        assert np.array_equal(dirty, bm.dirty_chunks(_host(sp)))
+        assert np.array_equal(scene.dense(), bm.dense())
