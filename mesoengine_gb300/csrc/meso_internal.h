@@ -114,7 +114,11 @@ meso_status scene_alloc(meso_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, uint6
 void scene_release(meso_ctx* ctx, meso_scene* s);
 // Recomputes the macro-cell map of a scene from its pointer grid: all cells,
 // or the n cells listed in d_cells (linear macro-cell indices).
-meso_status rebuild_macro(meso_ctx* ctx, meso_scene* s, const uint32_t* d_cells, uint32_t n, cudaStream_t st);
+// Recomputes the cell maps: every cell (lists null), or the listed cells of
+// 4^3, 16^3 and 64^3 bricks (each list sorted unique, children before parents).
+meso_status rebuild_macro(meso_ctx* ctx, meso_scene* s, const uint32_t* d_cells, uint32_t n, cudaStream_t st,
+                          const uint32_t* d_cells2 = nullptr, uint32_t n2 = 0, const uint32_t* d_cells3 = nullptr,
+                          uint32_t n3 = 0);
 
 // Kernel launchers (defined in the .cu files).
 meso_status launch_mesh(meso_ctx* ctx, const meso_mesh_source* src, const int32_t* d_coords,

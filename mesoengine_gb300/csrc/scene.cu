@@ -450,10 +450,12 @@ __global__ void macro_kernel(const uint32_t* ptr, int bx, int by, uint8_t* macro
 
 // One thread per 16x16x16-brick cell: any occupied 4x4x4-brick child -> 1; a
 // cell that extends past the grid is marked 1 too, so no jump leaves the grid.
-__global__ void macro2_kernel(const uint8_t* macro, int bx, int by, int bz, uint8_t* macro2) {
+__global__ void macro2_kernel(const uint8_t* macro, int bx, int by, int bz, uint8_t* macro2, const uint32_t* list,
+                              uint32_t n) {
   const int m2x = (bx + 15) / 16, m2y = (by + 15) / 16, m2z = (bz + 15) / 16;
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (uint32_t)(m2x * m2y * m2z)) return;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (list ? n : (uint32_t)(m2x * m2y * m2z))) return;
+  const uint32_t i = list ? list[t] : t;
   const int cx = (int)(i % (uint32_t)m2x), cy = (int)((i / (uint32_t)m2x) % (uint32_t)m2y), cz = (int)(i / ((uint32_t)m2x * m2y));
   const int mx = bx / 4, my = by / 4, mz = bz / 4;
   bool any = (cx + 1) * 4 > mx || (cy + 1) * 4 > my || (cz + 1) * 4 > mz;
@@ -466,10 +468,12 @@ __global__ void macro2_kernel(const uint8_t* macro, int bx, int by, int bz, uint
 
 // One thread per 64x64x64-brick cell: any nonzero 16x16x16 child, or a cell
 // extending past the grid -> 1.
-__global__ void macro3_kernel(const uint8_t* macro2, int bx, int by, int bz, uint8_t* macro3) {
+__global__ void macro3_kernel(const uint8_t* macro2, int bx, int by, int bz, uint8_t* macro3, const uint32_t* list,
+                              uint32_t n) {
   const int m3x = (bx + 63) / 64, m3y = (by + 63) / 64, m3z = (bz + 63) / 64;
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (uint32_t)(m3x * m3y * m3z)) return;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (list ? n : (uint32_t)(m3x * m3y * m3z))) return;
+  const uint32_t i = list ? list[t] : t;
   const int cx = (int)(i % (uint32_t)m3x), cy = (int)((i / (uint32_t)m3x) % (uint32_t)m3y), cz = (int)(i / ((uint32_t)m3x * m3y));
   const int m2x = (bx + 15) / 16, m2y = (by + 15) / 16;
   bool any = (cx + 1) * 64 > bx || (cy + 1) * 64 > by || (cz + 1) * 64 > bz;
@@ -534,15 +538,20 @@ void scene_release(meso_ctx* ctx, meso_scene* s) {
   delete s;
 }
 
-meso_status rebuild_macro(meso_ctx* ctx, meso_scene* s, const uint32_t* d_cells, uint32_t n, cudaStream_t st) {
+meso_status rebuild_macro(meso_ctx* ctx, meso_scene* s, const uint32_t* d_cells, uint32_t n, cudaStream_t st,
+                          const uint32_t* d_cells2, uint32_t n2, const uint32_t* d_cells3, uint32_t n3) {
   const uint64_t cells = d_cells ? n : n_macro_of(s);
   if (cells == 0) return MESO_OK;
   macro_kernel<<<(unsigned)((cells * 32 + 255) / 256), 256, 0, st>>>(s->d_ptr, s->bx, s->by, s->d_macro, d_cells,
                                                                      cells);
-  const uint64_t cells2 = n_macro2_of(s);
-  macro2_kernel<<<(unsigned)((cells2 + 255) / 256), 256, 0, st>>>(s->d_macro, s->bx, s->by, s->bz, s->d_macro2);
-  const uint64_t cells3 = n_macro3_of(s);
-  macro3_kernel<<<(unsigned)((cells3 + 255) / 256), 256, 0, st>>>(s->d_macro2, s->bx, s->by, s->bz, s->d_macro3);
+  const uint64_t cells2 = d_cells2 ? n2 : n_macro2_of(s);
+  if (cells2)
+    macro2_kernel<<<(unsigned)((cells2 + 255) / 256), 256, 0, st>>>(s->d_macro, s->bx, s->by, s->bz, s->d_macro2,
+                                                                     d_cells2, n2);
+  const uint64_t cells3 = d_cells3 ? n3 : n_macro3_of(s);
+  if (cells3)
+    macro3_kernel<<<(unsigned)((cells3 + 255) / 256), 256, 0, st>>>(s->d_macro2, s->bx, s->by, s->bz, s->d_macro3,
+                                                                     d_cells3, n3);
   ctx->launches.fetch_add(3);
   MESO_CUDA_TRY(cudaGetLastError());
   return MESO_OK;
@@ -797,29 +806,47 @@ meso_status edit_spheres(meso_ctx* ctx, meso_scene* s, const meso_sphere_edit* h
   if (h_dirty) std::copy(chunks.begin(), chunks.begin() + std::min<size_t>(chunks.size(), dirty_cap), h_dirty);
   if (bricks.empty()) return chunks.size() > dirty_cap && h_dirty ? fail(MESO_ERR_OVERFLOW, "edit: dirty list overflow") : MESO_OK;
   const size_t nb = bricks.size();
-  // macro cells holding the touched bricks (sorted unique)
-  std::vector<uint32_t> cells;
-  cells.reserve(nb);
-  for (uint32_t b : bricks) {
-    const uint32_t x = b % (uint32_t)s->bx, y = (b / (uint32_t)s->bx) % (uint32_t)s->by,
-                   z = b / ((uint32_t)s->bx * (uint32_t)s->by);
-    cells.push_back((x >> 2) + (uint32_t)(s->bx >> 2) * ((y >> 2) + (uint32_t)(s->by >> 2) * (z >> 2)));
+  // cells of 4^3, 16^3 and 64^3 bricks holding the touched bricks (sorted
+  // unique): only their emptiness bytes are recomputed
+  std::vector<uint32_t> cells[3];
+  const uint32_t BX = (uint32_t)s->bx, BY = (uint32_t)s->by;
+  const uint32_t gx[3] = {BX >> 2, (BX + 15) / 16, (BX + 63) / 64}, gy[3] = {BY >> 2, ((uint32_t)s->by + 15) / 16,
+                                                                          ((uint32_t)s->by + 63) / 64};
+  for (int l = 0; l < 3; l++) {
+    const int sh = 2 * (l + 1);
+    cells[l].reserve(nb);
+    for (uint32_t b : bricks) {
+      const uint32_t x = b % BX, y = (b / BX) % BY, z = b / (BX * BY);
+      cells[l].push_back((x >> sh) + gx[l] * ((y >> sh) + gy[l] * (z >> sh)));
+    }
+    std::sort(cells[l].begin(), cells[l].end());
+    cells[l].erase(std::unique(cells[l].begin(), cells[l].end()), cells[l].end());
   }
-  std::sort(cells.begin(), cells.end());
-  cells.erase(std::unique(cells.begin(), cells.end()), cells.end());
-  const size_t nc = cells.size();
-  const size_t bytes = n * sizeof(meso_sphere_edit) + nb * 4 + nb * 1024 + nb + 64 + nc * 4 + 16;
+  // device scratch: [spheres | bricks | cells | cells2 | cells3] uploaded in
+  // one copy, then the per-brick temporaries
+  const size_t nc = cells[0].size(), nc2 = cells[1].size(), nc3 = cells[2].size();
+  const size_t up = n * sizeof(meso_sphere_edit) + 4 * (nb + nc + nc2 + nc3);
+  const size_t up16 = (up + 15) & ~size_t(15);
+  std::vector<uint8_t> h(up);
+  std::memcpy(h.data(), h_sp, n * sizeof(meso_sphere_edit));
+  size_t o = n * sizeof(meso_sphere_edit);
+  std::memcpy(h.data() + o, bricks.data(), nb * 4);
+  o += nb * 4;
+  for (int l = 0; l < 3; l++) {
+    std::memcpy(h.data() + o, cells[l].data(), cells[l].size() * 4);
+    o += cells[l].size() * 4;
+  }
+  const size_t bytes = up16 + nb * 1024 + nb + 16;
   uint8_t* d = nullptr;
   MESO_CUDA_TRY(cudaMallocAsync(&d, bytes, st));
   meso_sphere_edit* d_sp = reinterpret_cast<meso_sphere_edit*>(d);
   uint32_t* d_b = reinterpret_cast<uint32_t*>(d + n * sizeof(meso_sphere_edit));
-  uint16_t* d_temp = reinterpret_cast<uint16_t*>(d + ((n * sizeof(meso_sphere_edit) + nb * 4 + 15) & ~size_t(15)));
+  uint32_t* d_cells = d_b + nb;
+  uint32_t* d_cells2 = d_cells + nc;
+  uint32_t* d_cells3 = d_cells2 + nc2;
+  uint16_t* d_temp = reinterpret_cast<uint16_t*>(d + up16);
   uint8_t* d_state = reinterpret_cast<uint8_t*>(d_temp) + nb * 1024;
-  uint32_t* d_cells = reinterpret_cast<uint32_t*>(d + ((n * sizeof(meso_sphere_edit) + nb * 4 + 15) & ~size_t(15)) +
-                                                  ((nb * 1024 + nb + 15) & ~size_t(15)));
-  cudaError_t ce = cudaMemcpyAsync(d_sp, h_sp, n * sizeof(meso_sphere_edit), cudaMemcpyHostToDevice, st);
-  if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_b, bricks.data(), nb * 4, cudaMemcpyHostToDevice, st);
-  if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_cells, cells.data(), nc * 4, cudaMemcpyHostToDevice, st);
+  const cudaError_t ce = cudaMemcpyAsync(d, h.data(), up, cudaMemcpyHostToDevice, st);
   if (ce != cudaSuccess) {
     cudaFreeAsync(d, st);
     return cuda_fail(ce, "edit: upload");
@@ -845,7 +872,8 @@ meso_status edit_spheres(meso_ctx* ctx, meso_scene* s, const meso_sphere_edit* h
   edit_alloc_kernel<<<blocks, 256, 0, st>>>(P);
   edit_fix_kernel<<<1, 1, 0, st>>>(P.alloc, P.capacity);
   ctx->launches.fetch_add(3);
-  const meso_status mrc = rebuild_macro(ctx, s, d_cells, (uint32_t)nc, st);
+  const meso_status mrc =
+      rebuild_macro(ctx, s, d_cells, (uint32_t)nc, st, d_cells2, (uint32_t)nc2, d_cells3, (uint32_t)nc3);
   MESO_CUDA_TRY(cudaFreeAsync(d, st));
   if (mrc != MESO_OK) return mrc;
   MESO_CUDA_TRY(cudaGetLastError());

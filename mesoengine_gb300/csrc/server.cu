@@ -303,7 +303,9 @@ void launch_batch(meso_server* srv, Slot& s) {
     rc = launch_raymarch(ctx, scenes.data(), cams.data(), (uint32_t)cams.size(), srv->light, s.reqs[0].req.flags,
                          s.d_hits, rs, s.d_table, s.table_bytes);
   if (rc == MESO_OK) {
-    dim3 grid(64, segs.n);
+    // about eight CTAs per SM over the batch, at least eight per request
+    const uint32_t per_seg = std::max<uint32_t>(8u, ((uint32_t)ctx->sm_count * 8u + segs.n - 1) / segs.n);
+    dim3 grid(std::min<uint32_t>(per_seg, 1024u), segs.n);
     hit_hash_kernel<<<grid, 256, 0, rs>>>(reinterpret_cast<const uint64_t*>(s.d_hits), segs, s.d_sums);
     ctx->launches.fetch_add(s.edit ? 2 : 1);
     if (s.edit) {
