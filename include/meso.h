@@ -431,9 +431,10 @@ meso_status meso_graph_destroy(meso_graph* graph);
 
 /* ------------------------------------------------------------------ tuning */
 
-/* Grid search over mesher CTAs per SM and chunks per ticket, and ray tile
- * shape and warps per CTA, on synthetic inputs; applies the best to ctx and
- * writes JSON to path (NULL = do not write). */
+/* Grid search over the mesher's chunks per queue ticket and the ray tile
+ * shape and warps per CTA, on synthetic inputs (the mesher keeps two 16-warp
+ * CTAs per SM, all that registers and shared memory allow); applies the best
+ * to ctx and writes JSON to path (NULL = do not write). */
 meso_status meso_autotune(meso_ctx* ctx, const char* path);
 
 #ifdef __cplusplus
