@@ -5,10 +5,14 @@ Headline step (value): one 1920x1080 frame of the 1024^3 sparse terrain scene
 (8^3 bricks under a 128^3 pointer grid, ~15% solid, uint16 materials),
 primary rays plus one shadow ray per hit towards normalize(0.3, 0.5, 0.8),
 FP32, one plain per-view launch; metric Mrays/s = (primary + shadow rays) / s.
+roofline.l2 gives the same algorithmic bytes against the L2 read bandwidth
+measured in the run (the raymarch's fetches hit in L2).
 Also reported on the same line:
   mesh        batched meshing of 4096 standalone 32^3 uint16 chunks (Gvox/s,
-              persistent kernel vs one launch per chunk, HBM roofline, CPU
-              oracle on the host cores with a bit-exact check);
+              persistent kernel vs one launch per chunk, directly and replayed
+              as a CUDA graph, HBM roofline, CPU oracle on the host cores
+              with a bit-exact check); mesh.uint8: the same chunks as uint8
+              and the 256^3 uint8 grid of the small plain case;
   served      the served raymarch stream: p50/p99 latency and Mrays/s at the
               offered load, capacity (requests submitted at once) and the
               plain form (one launch per request, waited for);
