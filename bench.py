@@ -27,8 +27,10 @@ Also reported on the same line:
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-N>1 runs independent replicas, one per rank (the path has no exchange step):
-value = rays of all ranks / the slowest rank's time.
+N>1 runs independent replicas, one per rank and GPU (the path has no
+exchange step): value = rays of all ranks / the slowest rank's time.  Under
+torchrun WORLD_SIZE must equal N; run directly, the script starts the N
+replica processes itself (gloo on 127.0.0.1 for the barrier and the max).
 """
 from __future__ import annotations
 
@@ -130,6 +132,23 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def spawn_replicas(n: int) -> int:
+    """Runs this command as n replica processes (RANK = LOCAL_RANK = 0..n-1,
+    rendezvous on 127.0.0.1) when it was not launched by torchrun; rank 0
+    prints the line.  Returns the worst exit code."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n), LOCAL_WORLD_SIZE=str(n),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__)] + sys.argv[1:], env=env))
+    rcs = [p.wait() for p in procs]
+    return max(rcs, key=abs)
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -210,11 +229,13 @@ def bench_raymarch(ctx, meso, steps, warmup, dist, clocks):
     fetches, bricks, nhits, traversals = ctx.raymarch_stats(scene, cam, out=out)
     algo_bytes = 4 * fetches + 64 * bricks + 2 * nhits + 24 * FRAME_W * FRAME_H
     info = scene.info()
+    solid = scene.count_solid()
     return {
         "scene": scene, "cam": cam, "hits": hits, "rays": rays, "ms": ms, "times": times,
         "launches": launches, "e2e_ms": e2e_ms, "algo_bytes": algo_bytes,
         "counts": {"pointer_fetches": fetches, "bricks_entered": bricks, "hits": nhits, "traversals": traversals},
         "bricks": int(info.n_bricks), "scene_bytes": int(info.device_bytes),
+        "occupancy": solid / float(t.nx * t.ny * t.nz),
     }
 
 
@@ -344,7 +365,55 @@ def bench_mesh_u8(ctx, meso, m, steps):
                         "gvox_s": round(512 * 32768 / (ms_b * 1e6), 2), "ms": round(ms_b, 4), "quads": q_b,
                         "per_chunk_launch_gvox_s": round(512 * 32768 / (ms_p * 1e6), 3),
                         "batched_over_per_launch": round(ms_p / ms_b, 2)}
+    res["dense_256"]["ray"] = bench_ray_dense256(ctx, meso, g, steps, flush)
     return res
+
+
+CFG1_ORIGIN, CFG1_TARGET, CFG1_W, CFG1_H = (-160.0, -96.0, 384.0), (128.0, 128.0, 128.0), 640, 360
+
+
+def bench_ray_dense256(ctx, meso, grid, steps, flush):
+    """The small plain case's raymarch: the 256^3 uint8 grid as a brick map
+    (built on the device from the generated grid), one 640x360 pinhole camera
+    (60 degree vertical FOV) outside the grid aimed at its centre, primary
+    rays to the first hit; one launch per step, L2 flushed between steps.
+    The oracle DDA traces the same frame on all host cores beside it."""
+    import oracle
+    scene = ctx.scene_from_grid(meso.SRC_GRID_U8, grid, (256, 256, 256))
+    cam = meso.camera(CFG1_ORIGIN, CFG1_TARGET, CFG1_W, CFG1_H)
+    out = ctx.alloc(CFG1_W * CFG1_H * 24)
+    for _ in range(3):
+        ctx.raymarch(scene, cam, shadow=False, out=out, download=False)
+    evs = [(ctx.event(), ctx.event()) for _ in range(steps)]
+    for a, b in evs:
+        flush.zero()
+        ctx.record(a)
+        ctx.raymarch(scene, cam, shadow=False, out=out, download=False)
+        ctx.record(b)
+    ctx.sync()
+    ms = sum(ctx.elapsed_ms(a, b) for a, b in evs) / steps
+    hits = out.download(meso.HIT_DTYPE, CFG1_W * CFG1_H)
+    solid = scene.count_solid()
+    host = oracle.gen_dense_u8(256, 256, 256, 1)
+    bm = oracle.HostBrickMap.from_dense(host.astype(np.uint16))
+    threads = oracle.hardware_threads()
+    ocam = oracle.camera(CFG1_ORIGIN, CFG1_TARGET, CFG1_W, CFG1_H)
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        ref = oracle.raymarch(bm, ocam, shadow=False, nthreads=threads)
+        reps += 1
+        if time.perf_counter() - t0 > 2.0 or reps >= 20:
+            break
+    cpu_s = (time.perf_counter() - t0) / reps
+    scene.destroy()
+    rays = CFG1_W * CFG1_H
+    return {"workload": "256^3 uint8 grid as a brick map, 640x360 pinhole camera (60 deg vertical FOV) from "
+                        f"{CFG1_ORIGIN} aimed at {CFG1_TARGET}, primary rays to the first hit, one launch",
+            "mrays_s": round(rays / (ms * 1e3), 1), "ms": round(ms, 4), "rays": rays,
+            "hits": int(np.isfinite(hits["t"]).sum()), "occupancy": round(solid / 256 ** 3, 4),
+            "parity_bit_exact": bool(np.array_equal(hits.view(np.uint8), ref.view(np.uint8))),
+            "cpu_baseline": {"value": round(rays / cpu_s / 1e6, 2), "unit": "Mrays/s", "cores": threads,
+                             "kind": "port", "sample": f"the full 640x360 frame, {reps} runs of {cpu_s * 1e3:.1f} ms"}}
 
 
 def cpu_mesh_baseline(m, n_single=512):
@@ -547,6 +616,7 @@ def bench_serve_edit(ctx, meso, seconds, rate=200.0):
     remesh of the dirty 32^3 chunks, then a 1920x1080 render (primary)."""
     t = meso.terrain_preset("edit4096")
     scene = ctx.scene_from_terrain(t, spare_bricks=4 << 20)
+    occupancy = scene.count_solid() / float(t.nx * t.ny * t.nz)
     n = t.nx
     rng = np.random.default_rng(9)
     items = []
@@ -573,6 +643,7 @@ def bench_serve_edit(ctx, meso, seconds, rate=200.0):
     res["gvox_meshed_s_busy"] = round(chunks * 32768 / max(busy, 1e-9) / 1e9, 3)
     res["workload"] = (f"4096^3 terrain (512^3 pointer grid), Poisson {rate:.0f} req/s for {seconds:.0f} s (seed 9), "
                        "1-32 sphere edits + remesh of dirty chunks + 1920x1080 primary render")
+    res["voxel_occupancy"] = round(occupancy, 5)
     # capacity (requests submitted at once) and the plain form (edit, one mesh
     # launch per dirty chunk, one render launch, waited for) on fresh copies
     k = min(200, len(items))
@@ -675,6 +746,8 @@ def run_ours(args, world, rank, local, dist):
                      f"{r['bricks']} bricks, {r['scene_bytes'] / 2**20:.0f} MiB resident",
             "camera": {"origin": CAM_ORIGIN, "target": CAM_TARGET, "fov_y_deg": 60},
             "rays_per_frame": r["rays"],
+            "voxel_occupancy": round(r["occupancy"], 4),
+            "tuning": {k: v for k, v in ctx.config().items() if k not in ("device", "hbm_budget_bytes")},
             "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB memset outside the timed events)",
             "parallelism": f"replicas x{world}",
         },
@@ -800,6 +873,12 @@ def main():
         run_profile_case(args.profile)
         return
     args.warmup = max(3, args.warmup)
+    if args.gpus < 1:
+        ap.error("--gpus must be at least 1")
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(spawn_replicas(args.gpus))
+    if int(os.environ.get("WORLD_SIZE", "1")) != args.gpus:
+        ap.error(f"--gpus {args.gpus} but WORLD_SIZE={os.environ.get('WORLD_SIZE')}: one process per GPU")
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank, local, dist)

@@ -77,6 +77,9 @@ void meso_ctx_destroy(meso_ctx* ctx);
 const char* meso_last_error_string(void);
 const char* meso_status_string(meso_status s);
 meso_status meso_sync(meso_ctx* ctx, void* stream);
+/* The context's effective configuration: defaults filled in, tuning file
+ * and autotuning applied (tuning_path is returned as NULL). */
+meso_status meso_ctx_get_config(const meso_ctx* ctx, meso_config* out);
 /* Number of mesher/raymarch/scene kernels this context has launched. */
 uint64_t meso_kernel_launches(const meso_ctx* ctx);
 int meso_sm_count(const meso_ctx* ctx);
@@ -148,6 +151,18 @@ meso_status meso_scene_create_terrain(meso_ctx* ctx, const meso_terrain* t, uint
  * its brick map on the device. */
 meso_status meso_scene_create_dense(meso_ctx* ctx, const uint16_t* h_grid, int32_t nx, int32_t ny,
                                     int32_t nz, uint64_t spare_bricks, meso_scene** out);
+/* Builds the brick map of a dense grid already in device memory: kind
+ * MESO_SRC_GRID_U8 (uint8 materials, widened to uint16) or MESO_SRC_GRID_U16;
+ * x fastest, dims multiples of 32.  Lets a grid made on the device (e.g. by
+ * meso_generate_dense_u8) be raymarched without a host round trip; the
+ * reference's counterpart is the same pool write as for the terrain
+ * (Runtimes/Voxel/Chunk/ChunkPool.h:623-628).  d_grid is only read. */
+meso_status meso_scene_create_grid(meso_ctx* ctx, int32_t kind, const void* d_grid, int32_t nx, int32_t ny,
+                                   int32_t nz, uint64_t spare_bricks, meso_scene** out);
+/* Solid voxels of a scene (set occupancy bits of its linked bricks); for
+ * reporting occupancy (no counterpart in the reference).  Waits for the
+ * context's stream. */
+meso_status meso_scene_count_solid(meso_ctx* ctx, const meso_scene* scene, uint64_t* n_solid);
 meso_status meso_scene_destroy(meso_ctx* ctx, meso_scene* scene);
 meso_status meso_scene_get_info(meso_ctx* ctx, const meso_scene* scene, meso_scene_info* info);
 /* Copies the scene to the host: ptr has (nx/8)(ny/8)(nz/8) entries; occ and
@@ -287,13 +302,16 @@ meso_status meso_raymarch_stats(meso_ctx* ctx, const meso_scene* const* scenes, 
  * call -- a frame loop on a fixed device-memory budget that must not
  * allocate mid-frame (an allocation can synchronise the device and stall the
  * frame), or a host application whose own memory manager owns all device
- * memory -- the view descriptors go to a fixed 64 KiB device array instead
- * of a per-call allocation.  At most 512 views per call (more returns
- * MESO_ERR_INVALID_ARG).  The array stays resident on every device that
- * loads the library until the process exits.  The first call on a device
- * looks up the array's address and caches it; make that first call before
- * any stream capture.  All calls share the array: calls whose kernels
- * overlap on the GPU race on it, so keep them on one stream or order them. */
+ * memory -- the view descriptors go to a fixed device array of 512 x 152
+ * bytes (76 KiB) instead of a per-call allocation; they travel there as
+ * kernel parameters, 64 views at a time (9.5 KiB of the caller's stack).
+ * At most 512 views per call (more returns MESO_ERR_INVALID_ARG).  The array
+ * stays resident on every device that loads the library until the process
+ * exits.  The calling thread's current device must be the context's device
+ * (else MESO_ERR_INVALID_ARG).  The first call on a device looks up the
+ * array's address and caches it; make that first call before any stream
+ * capture.  All calls share the array: calls whose kernels overlap on the
+ * GPU race on it, so keep them on one stream or order them. */
 meso_status meso_raymarch_noalloc(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* h_cams,
                                   uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
                                   void* stream);
@@ -431,10 +449,14 @@ meso_status meso_graph_destroy(meso_graph* graph);
 
 /* ------------------------------------------------------------------ tuning */
 
-/* Grid search over the mesher's chunks per queue ticket and the ray tile
- * shape and warps per CTA, on synthetic inputs (the mesher keeps two 16-warp
- * CTAs per SM, all that registers and shared memory allow); applies the best
- * to ctx and writes JSON to path (NULL = do not write). */
+/* Grid search on synthetic inputs, standing in for the hand-set
+ * ChunkTaskPerCore / MaxUnsyncedLoadChunkCount (Runtimes/Voxel/VoxelSceneConfig.h:35-37):
+ * the ray tile shape (lanes along x, warps per CTA) on a 1280x720 view of a
+ * 512^3 terrain, and the mesher's CTAs per SM (1 or 2; a CTA meshes one
+ * 32^3 chunk = 64 bricks at a time, so this sets the bricks in flight per
+ * SM) and chunks per queue ticket on 1024 generated chunks.  Applies the
+ * fastest to ctx and writes flat JSON to path (NULL = do not write), which
+ * meso_config.tuning_path reads back. */
 meso_status meso_autotune(meso_ctx* ctx, const char* path);
 
 #ifdef __cplusplus

@@ -131,6 +131,7 @@ _lib = None
 _SIGNATURES = {
     "meso_ctx_create": [ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_void_p)],
     "meso_ctx_destroy": [ctypes.c_void_p],
+    "meso_ctx_get_config": [ctypes.c_void_p, ctypes.POINTER(Config)],
     "meso_sync": [ctypes.c_void_p, ctypes.c_void_p],
     "meso_dev_alloc": [ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)],
     "meso_dev_free": [ctypes.c_void_p, ctypes.c_void_p],
@@ -149,6 +150,9 @@ _SIGNATURES = {
                                   ctypes.POINTER(ctypes.c_void_p)],
     "meso_scene_create_dense": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                 ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)],
+    "meso_scene_create_grid": [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                               ctypes.c_int32, ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)],
+    "meso_scene_count_solid": [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)],
     "meso_scene_destroy": [ctypes.c_void_p, ctypes.c_void_p],
     "meso_scene_get_info": [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(SceneInfo)],
     "meso_scene_download": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
@@ -324,6 +328,12 @@ class Scene:
         i = self.info()
         return (i.nx, i.ny, i.nz)
 
+    def count_solid(self) -> int:
+        """Solid voxels of the scene (counted on the device)."""
+        n = ctypes.c_uint64()
+        _check(_lib.meso_scene_count_solid(self.ctx.handle, self.handle, ctypes.byref(n)))
+        return int(n.value)
+
     def download(self):
         """(ptr, occ[cap,8], mat[cap,512]) host copies."""
         i = self.info()
@@ -434,6 +444,13 @@ class Context:
         nz, ny, nx = g.shape
         h = ctypes.c_void_p()
         _check(_lib.meso_scene_create_dense(self.handle, _np_ptr(g), nx, ny, nz, spare_bricks, ctypes.byref(h)))
+        return Scene(self, h.value)
+
+    def scene_from_grid(self, kind: int, grid: "DeviceBuffer", dims, spare_bricks: int = 0) -> Scene:
+        """Brick map of a dense device grid (SRC_GRID_U8 or SRC_GRID_U16), dims (nx, ny, nz)."""
+        nx, ny, nz = dims
+        h = ctypes.c_void_p()
+        _check(_lib.meso_scene_create_grid(self.handle, kind, grid.ptr, nx, ny, nz, spare_bricks, ctypes.byref(h)))
         return Scene(self, h.value)
 
     # -- generators
@@ -610,6 +627,13 @@ class Context:
 
     def autotune(self, path: str | None = None) -> None:
         _check(_lib.meso_autotune(self.handle, path.encode() if path else None))
+
+    def config(self) -> dict:
+        """The effective launch configuration (defaults, tuning file and autotuning applied)."""
+        c = Config()
+        _check(_lib.meso_ctx_get_config(self.handle, ctypes.byref(c)))
+        return {k: getattr(c, k) for k in ("device", "mesh_ctas_per_sm", "mesh_chunks_per_ticket", "ray_tile_w",
+                                            "ray_tile_h", "ray_warps_per_cta", "hbm_budget_bytes")}
 
     def close(self) -> None:
         if getattr(self, "handle", None) and _lib is not None:

@@ -30,6 +30,8 @@ meso_status cuda_fail(cudaError_t e, const char* what) {
 // defined in scene.cu
 meso_status scene_create_terrain(meso_ctx*, const meso_terrain*, uint64_t, meso_scene**);
 meso_status scene_create_dense(meso_ctx*, const uint16_t*, int32_t, int32_t, int32_t, uint64_t, meso_scene**);
+meso_status scene_create_grid(meso_ctx*, int32_t, const void*, int32_t, int32_t, int32_t, uint64_t, meso_scene**);
+meso_status scene_count_solid(meso_ctx*, const meso_scene*, uint64_t*);
 meso_status generate_dense_u8(meso_ctx*, int32_t, int32_t, int32_t, uint32_t, uint8_t*, cudaStream_t);
 meso_status generate_chunks_u16(meso_ctx*, uint32_t, uint32_t, uint16_t*, uint32_t*, cudaStream_t);
 meso_status edit_spheres(meso_ctx*, meso_scene*, const meso_sphere_edit*, uint32_t, uint32_t*, uint32_t, uint32_t*,
@@ -237,6 +239,22 @@ meso_status meso_measure_l2_read(meso_ctx* ctx, uint64_t bytes, uint32_t passes,
   return MESO_OK;
 }
 
+meso_status meso_ctx_get_config(const meso_ctx* ctx, meso_config* out) {
+  if (!ctx || !out) return fail(MESO_ERR_INVALID_ARG, "ctx_get_config: null argument");
+  memset(out, 0, sizeof(*out));
+  out->chunk_edge = 32;
+  out->brick_edge = 8;
+  out->device = ctx->device;
+  out->mesh_ctas_per_sm = ctx->tuning.mesh_ctas_per_sm ? ctx->tuning.mesh_ctas_per_sm : 2;
+  out->mesh_chunks_per_ticket = ctx->tuning.mesh_chunks_per_ticket ? ctx->tuning.mesh_chunks_per_ticket : 1;
+  out->ray_tile_w = ctx->tuning.ray_tile_w ? ctx->tuning.ray_tile_w : 8;
+  out->ray_tile_h = 32 / out->ray_tile_w;
+  out->ray_warps_per_cta = ctx->tuning.ray_warps_per_cta ? ctx->tuning.ray_warps_per_cta : 4;
+  out->hbm_budget_bytes = ctx->budget_bytes;
+  out->tuning_path = nullptr;
+  return MESO_OK;
+}
+
 uint64_t meso_kernel_launches(const meso_ctx* ctx) { return ctx ? ctx->launches.load() : 0; }
 int meso_sm_count(const meso_ctx* ctx) { return ctx ? ctx->sm_count : 0; }
 
@@ -320,6 +338,18 @@ meso_status meso_scene_create_dense(meso_ctx* ctx, const uint16_t* h_grid, int32
   if (!ctx) return fail(MESO_ERR_INVALID_ARG, "null ctx");
   std::lock_guard<std::mutex> lk(ctx->mu);
   return scene_create_dense(ctx, h_grid, nx, ny, nz, spare, out);
+}
+
+meso_status meso_scene_create_grid(meso_ctx* ctx, int32_t kind, const void* d_grid, int32_t nx, int32_t ny,
+                                   int32_t nz, uint64_t spare, meso_scene** out) {
+  if (!ctx) return fail(MESO_ERR_INVALID_ARG, "null ctx");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  return scene_create_grid(ctx, kind, d_grid, nx, ny, nz, spare, out);
+}
+
+meso_status meso_scene_count_solid(meso_ctx* ctx, const meso_scene* scene, uint64_t* n_solid) {
+  if (!ctx) return fail(MESO_ERR_INVALID_ARG, "null ctx");
+  return scene_count_solid(ctx, scene, n_solid);
 }
 
 meso_status meso_scene_destroy(meso_ctx* ctx, meso_scene* scene) {

@@ -565,11 +565,12 @@ size_t raymarch_view_table_bytes(uint32_t n_views) { return sizeof(RayView) * (s
 // frame into device memory is unchanged).
 static uint32_t block_order_mul(uint32_t blocks) { return blocks > 1 && blocks % 7919u ? 7919u : 0u; }
 
-// Fills view descriptors (host) for n_views cameras; returns total tiles.
-static uint64_t fill_views(const meso_scene* const* scenes, const meso_camera* cams, uint32_t n_views, uint32_t tw,
-                           uint32_t th, RayView* out) {
-  uint64_t tiles = 0, hits = 0;
-  for (uint32_t v = 0; v < n_views; v++) {
+// Fills the host descriptors out[0 .. n) of views scenes/cams[0 .. n).  tiles
+// and hits are running totals over all views of the launch (in: those of
+// the views before these; out: including them).
+static void fill_views(const meso_scene* const* scenes, const meso_camera* cams, uint32_t n, uint32_t tw, uint32_t th,
+                       RayView* out, uint64_t& tiles, uint64_t& hits) {
+  for (uint32_t v = 0; v < n; v++) {
     const meso_scene* s = scenes[v];
     const meso_camera& c = cams[v];
     RayView& V = out[v];
@@ -601,7 +602,49 @@ static uint64_t fill_views(const meso_scene* const* scenes, const meso_camera* c
     tiles += (uint64_t)V.tiles_x * tiles_y;
     hits += (uint64_t)c.width * c.height;
   }
-  return tiles;
+}
+
+}  // namespace meso
+
+namespace meso {
+namespace {
+
+// Descriptors of up to kFillViews views, passed by value to the kernel that
+// writes them into a device view table.  Kernel parameters are copied when
+// the launch is issued (and kept by value in a captured graph node), so no
+// host buffer has to outlive the call; 64 views are 9.5 KiB of parameters
+// and of the caller's stack.
+constexpr uint32_t kFillViews = 64;
+struct ViewBatch {
+  RayView v[kFillViews];
+};
+static_assert(sizeof(ViewBatch) <= 32000, "a view batch must fit the kernel parameter space");
+
+__global__ void view_fill_kernel(const __grid_constant__ ViewBatch b, uint32_t n, RayView* dst) {
+  const uint32_t words = n * (uint32_t)(sizeof(RayView) / 8);
+  const uint64_t* src = reinterpret_cast<const uint64_t*>(b.v);
+  uint64_t* d = reinterpret_cast<uint64_t*>(dst);
+  for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) d[i] = src[i];
+}
+
+}  // namespace
+
+// Writes the descriptors of n_views views into the device table d_table,
+// stream-ordered before the launch that reads it: one small kernel per 64
+// views, the descriptors travelling as its parameters.  *tiles receives the
+// total tiles of the views.
+static meso_status stage_view_table(const meso_scene* const* scenes, const meso_camera* cams, uint32_t n_views,
+                                    uint32_t tw, uint32_t th, RayView* d_table, cudaStream_t st, uint64_t* tiles) {
+  ViewBatch batch;
+  uint64_t t = 0, hits = 0;
+  for (uint32_t v0 = 0; v0 < n_views; v0 += kFillViews) {
+    const uint32_t n = n_views - v0 < kFillViews ? n_views - v0 : kFillViews;
+    fill_views(scenes + v0, cams + v0, n, tw, th, batch.v, t, hits);
+    view_fill_kernel<<<1, 128, 0, st>>>(batch, n, d_table + v0);
+    MESO_CUDA_TRY(cudaGetLastError());
+  }
+  *tiles = t;
+  return MESO_OK;
 }
 
 meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* cams,
@@ -636,7 +679,9 @@ meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, cons
   uint64_t tiles;
   if (n_views <= (uint32_t)kInlineViews) {
     InlineViews iv;
-    tiles = fill_views(scenes, cams, n_views, tw, th, iv.v);
+    tiles = 0;
+    uint64_t hits = 0;
+    fill_views(scenes, cams, n_views, tw, th, iv.v, tiles, hits);
     if (tiles >= (1ull << 31)) return fail(MESO_ERR_INVALID_ARG, "raymarch: too many tiles");
     P.total_tiles = (uint32_t)tiles;
     const uint32_t blocks = (uint32_t)((tiles + wpc - 1) / wpc);
@@ -646,14 +691,10 @@ meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, cons
   } else {
     if (!d_view_table || view_table_bytes < raymarch_view_table_bytes(n_views))
       return fail(MESO_ERR_INVALID_ARG, "raymarch: view table too small");
-    std::vector<RayView> host(n_views);
-    tiles = fill_views(scenes, cams, n_views, tw, th, host.data());
+    MESO_TRY(stage_view_table(scenes, cams, n_views, tw, th, static_cast<RayView*>(d_view_table), st, &tiles));
     if (tiles >= (1ull << 31)) return fail(MESO_ERR_INVALID_ARG, "raymarch: too many tiles");
     P.total_tiles = (uint32_t)tiles;
     P.table = static_cast<const RayView*>(d_view_table);
-    MESO_CUDA_TRY(cudaMemcpyAsync(d_view_table, host.data(), raymarch_view_table_bytes(n_views),
-                                  cudaMemcpyHostToDevice, st));
-    // the pageable copy above is staged before the call returns
     const uint32_t blocks = (uint32_t)((tiles + wpc - 1) / wpc);
     P.order_mul = block_order_mul(blocks);
     if (d_stats) raymarch_kernel<false, true><<<blocks, wpc * 32, 0, st>>>(P, empty_views);
@@ -675,13 +716,15 @@ meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, cons
 // must not allocate mid-frame (an allocation can synchronise the device and
 // stall the frame), or a host application whose own memory manager owns all
 // device memory.  This entry point keeps the table in a fixed file-scope
-// device array instead, and stages the descriptors on the host stack.
+// device array instead; the descriptors reach it as kernel parameters, 64
+// views at a time, through a 9.5 KiB batch on the caller's stack.
 //
 // Limits and behaviour:
 //  - at most kNoAllocViews (512) views per call; more is rejected with
 //    MESO_ERR_INVALID_ARG;
-//  - the array (64 KiB) stays resident on every device that loads the
-//    library until the process exits;
+//  - the array (512 x 152 B = 76 KiB) stays resident on every device that
+//    loads the library until the process exits;
+//  - the calling thread's current device must be the context's device;
 //  - the first call on a device looks up the array's device address (with
 //    that device current) and caches it; make that first call before any
 //    stream capture;
@@ -692,22 +735,20 @@ namespace meso {
 namespace {
 
 constexpr uint32_t kNoAllocViews = 512;
+static_assert(sizeof(RayView) == 152, "the documented size of the fixed view table is 512 x 152 bytes");
 static __device__ __align__(256) unsigned char g_noalloc_views[kNoAllocViews * sizeof(RayView)];
 
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[64] = {};
 
-// Device address of g_noalloc_views on `device` (looked up once per device).
+// Device address of g_noalloc_views on `device` (looked up once per device;
+// `device` is current when this is called).
 meso_status noalloc_table(int device, void** out) {
   if (device < 0 || device >= 64) return fail(MESO_ERR_INVALID_ARG, "raymarch_noalloc: device ordinal >= 64");
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
   if (!g_noalloc_ptr[device]) {
-    int prev = 0;
-    MESO_CUDA_TRY(cudaGetDevice(&prev));
-    if (prev != device) MESO_CUDA_TRY(cudaSetDevice(device));
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_views);
-    if (prev != device) cudaSetDevice(prev);
     if (e != cudaSuccess) return cuda_fail(e, "raymarch_noalloc: cudaGetSymbolAddress");
     g_noalloc_ptr[device] = p;
   }
@@ -736,10 +777,16 @@ extern "C" meso_status meso_raymarch_noalloc(meso_ctx* ctx, const meso_scene* co
   if (32 % tw) return fail(MESO_ERR_INVALID_ARG, "raymarch_noalloc: tile width must divide 32");
   const uint32_t th = 32 / tw;
   const uint32_t wpc = ctx->tuning.ray_warps_per_cta ? ctx->tuning.ray_warps_per_cta : 4;
+  int cur = -1;
+  MESO_CUDA_TRY(cudaGetDevice(&cur));
+  if (cur != ctx->device)
+    return fail(MESO_ERR_INVALID_ARG, "raymarch_noalloc: the current device is not the context's device");
   void* table = nullptr;
   MESO_TRY(noalloc_table(ctx->device, &table));
-  RayView host[kNoAllocViews];
-  const uint64_t tiles = fill_views(scenes, h_cams, n_views, tw, th, host);
+  // the same validation as meso_raymarch, before any work is issued
+  uint64_t tiles = 0;
+  for (uint32_t v = 0; v < n_views; v++)
+    tiles += (uint64_t)((h_cams[v].width + tw - 1) / tw) * ((h_cams[v].height + th - 1) / th);
   if (tiles >= (1ull << 31)) return fail(MESO_ERR_INVALID_ARG, "raymarch_noalloc: too many tiles");
   RayParams P;
   memset(&P, 0, sizeof(P));
@@ -756,8 +803,7 @@ extern "C" meso_status meso_raymarch_noalloc(meso_ctx* ctx, const meso_scene* co
     }
   P.hits = d_hits;
   const cudaStream_t st = pick_stream(ctx, stream);
-  // pageable source: the copy is staged before cudaMemcpyAsync returns
-  MESO_CUDA_TRY(cudaMemcpyAsync(table, host, sizeof(RayView) * (size_t)n_views, cudaMemcpyHostToDevice, st));
+  MESO_TRY(stage_view_table(scenes, h_cams, n_views, tw, th, static_cast<RayView*>(table), st, &tiles));
   static InlineViews unused_inline;  // zero-initialised; the table path does not read it
   const uint32_t blocks = (uint32_t)((tiles + wpc - 1) / wpc);
   P.order_mul = block_order_mul(blocks);

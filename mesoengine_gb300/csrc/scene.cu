@@ -210,7 +210,9 @@ meso_status number_bricks(meso_ctx* ctx, const uint8_t* d_flags, uint64_t nb, ui
 }
 
 // ---------------------------------------------------------- dense -> bricks
-__global__ void dense_flag_kernel(const uint16_t* grid, int nx, int ny, int nz, uint8_t* flags) {
+// T: uint16_t or uint8_t materials of a dense grid (x fastest).
+template <typename T>
+__global__ void dense_flag_kernel(const T* grid, int nx, int ny, int nz, uint8_t* flags) {
   const int bx = nx / 8, by = ny / 8, bz = nz / 8;
   const uint64_t nb = (uint64_t)bx * by * bz;
   const int lane = threadIdx.x & 31;
@@ -228,7 +230,8 @@ __global__ void dense_flag_kernel(const uint16_t* grid, int nx, int ny, int nz, 
   }
 }
 
-__global__ void dense_fill_kernel(const uint16_t* grid, int nx, int ny, int nz, const uint32_t* ptr, uint64_t* occ,
+template <typename T>
+__global__ void dense_fill_kernel(const T* grid, int nx, int ny, int nz, const uint32_t* ptr, uint64_t* occ,
                                   uint16_t* mat) {
   const int bx = nx / 8, by = ny / 8, bz = nz / 8;
   const uint64_t nb = (uint64_t)bx * by * bz;
@@ -241,7 +244,7 @@ __global__ void dense_fill_kernel(const uint16_t* grid, int nx, int ny, int nz, 
     for (int k = 0; k < 16; k++) {
       const int i = lane + 32 * k;
       const size_t g = (size_t)(X * 8 + (i & 7)) + (size_t)nx * ((size_t)(Y * 8 + ((i >> 3) & 7)) + (size_t)ny * (Z * 8 + (i >> 6)));
-      const uint16_t m = grid[g];
+      const uint16_t m = (uint16_t)grid[g];
       mat[(size_t)slot * 512 + i] = m;
       const uint32_t bits = __ballot_sync(kFull, m != 0);
       if (lane == 0) reinterpret_cast<uint32_t*>(occ + (size_t)slot * 8)[k] = bits;
@@ -419,6 +422,26 @@ __global__ void edit_alloc_kernel(EditParams P) {
 __global__ void edit_fix_kernel(int32_t* alloc, uint32_t capacity) {
   if (alloc[1] < 0) alloc[1] = 0;
   if ((uint32_t)alloc[0] > capacity) alloc[0] = (int32_t)capacity;
+}
+
+// Solid voxels of the live bricks: popcount of each linked brick's 8
+// occupancy words, summed per warp and added to *count.
+__global__ void count_solid_kernel(const uint32_t* ptr, uint64_t nb, const uint64_t* occ,
+                                   unsigned long long* count) {
+  uint32_t acc = 0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; b < nb; b += stride) {
+    const uint32_t p = ptr[b];
+    if (p == MESO_EMPTY_BRICK) continue;
+    const uint4* w = reinterpret_cast<const uint4*>(occ + (size_t)p * 8);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const uint4 v = w[k];
+      acc += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+    }
+  }
+  const uint32_t tot = __reduce_add_sync(kFull, acc);
+  if ((threadIdx.x & 31) == 0 && tot) atomicAdd(count, (unsigned long long)tot);
 }
 
 unsigned grid_for(uint64_t warps, int threads = 256) {
@@ -631,29 +654,23 @@ meso_status scene_create_terrain(meso_ctx* ctx, const meso_terrain* t, uint64_t 
   return MESO_OK;
 }
 
-meso_status scene_create_dense(meso_ctx* ctx, const uint16_t* h_grid, int32_t nx, int32_t ny, int32_t nz,
-                               uint64_t spare, meso_scene** out) {
-  if (!h_grid || !out) return fail(MESO_ERR_INVALID_ARG, "dense scene: null argument");
-  if (nx <= 0 || ny <= 0 || nz <= 0 || nx % 32 || ny % 32 || nz % 32 || nx > 8192 || ny > 8192 || nz > 8192)
-    return fail(MESO_ERR_INVALID_ARG, "dense scene: dims must be positive multiples of 32 (<= 8192)");
-  cudaStream_t st = ctx->stream;
-  const uint64_t nvox = (uint64_t)nx * ny * nz;
-  const uint64_t nb = nvox / 512;
-  uint16_t* d_grid = nullptr;
+// Brick map of a dense grid already in device memory (T = uint8_t or
+// uint16_t; a uint8 material m becomes the uint16 material m).
+template <typename T>
+static meso_status build_from_device_grid(meso_ctx* ctx, const T* d_grid, int32_t nx, int32_t ny, int32_t nz,
+                                          uint64_t spare, cudaStream_t st, meso_scene** out) {
+  const uint64_t nb = (uint64_t)nx * ny * nz / 512;
   uint8_t* d_flags = nullptr;
   uint32_t* d_ptr_tmp = nullptr;
-  cudaError_t ae = cudaMallocAsync(&d_grid, nvox * 2, st);
-  if (ae == cudaSuccess) ae = cudaMallocAsync(&d_flags, nb, st);
+  cudaError_t ae = cudaMallocAsync(&d_flags, nb, st);
   if (ae == cudaSuccess) ae = cudaMallocAsync(&d_ptr_tmp, nb * 4, st);
-  if (ae == cudaSuccess) ae = cudaMemcpyAsync(d_grid, h_grid, nvox * 2, cudaMemcpyHostToDevice, st);
   if (ae != cudaSuccess) {
-    cudaFreeAsync(d_grid, st);  // cudaFreeAsync(nullptr) is a no-op
-    cudaFreeAsync(d_flags, st);
+    cudaFreeAsync(d_flags, st);  // cudaFreeAsync(nullptr) is a no-op
     cudaFreeAsync(d_ptr_tmp, st);
     cudaStreamSynchronize(st);
-    return cuda_fail(ae, "dense scene: scratch allocation or upload");
+    return cuda_fail(ae, "dense scene: scratch allocation");
   }
-  dense_flag_kernel<<<grid_for(nb), 256, 0, st>>>(d_grid, nx, ny, nz, d_flags);
+  dense_flag_kernel<T><<<grid_for(nb), 256, 0, st>>>(d_grid, nx, ny, nz, d_flags);
   ctx->launches.fetch_add(1);
   uint64_t count = 0;
   meso_status rc = number_bricks(ctx, d_flags, nb, d_ptr_tmp, st, &count);
@@ -661,11 +678,10 @@ meso_status scene_create_dense(meso_ctx* ctx, const uint16_t* h_grid, int32_t nx
   if (rc == MESO_OK) rc = alloc_sized(ctx, nx, ny, nz, count, spare, &s);
   if (rc == MESO_OK) {
     cudaMemcpyAsync(s->d_ptr, d_ptr_tmp, nb * 4, cudaMemcpyDeviceToDevice, st);
-    dense_fill_kernel<<<grid_for(nb), 256, 0, st>>>(d_grid, nx, ny, nz, s->d_ptr, s->d_occ, s->d_mat);
+    dense_fill_kernel<T><<<grid_for(nb), 256, 0, st>>>(d_grid, nx, ny, nz, s->d_ptr, s->d_occ, s->d_mat);
     ctx->launches.fetch_add(1);
     rc = finish_pools(ctx, s, count, st);
   }
-  cudaFreeAsync(d_grid, st);
   cudaFreeAsync(d_flags, st);
   cudaFreeAsync(d_ptr_tmp, st);
   cudaError_t e = cudaStreamSynchronize(st);
@@ -675,6 +691,68 @@ meso_status scene_create_dense(meso_ctx* ctx, const uint16_t* h_grid, int32_t nx
     return rc;
   }
   *out = s;
+  return MESO_OK;
+}
+
+static meso_status check_grid_dims(int32_t nx, int32_t ny, int32_t nz) {
+  if (nx <= 0 || ny <= 0 || nz <= 0 || nx % 32 || ny % 32 || nz % 32 || nx > 8192 || ny > 8192 || nz > 8192)
+    return fail(MESO_ERR_INVALID_ARG, "dense scene: dims must be positive multiples of 32 (<= 8192)");
+  return MESO_OK;
+}
+
+meso_status scene_create_dense(meso_ctx* ctx, const uint16_t* h_grid, int32_t nx, int32_t ny, int32_t nz,
+                               uint64_t spare, meso_scene** out) {
+  if (!h_grid || !out) return fail(MESO_ERR_INVALID_ARG, "dense scene: null argument");
+  MESO_TRY(check_grid_dims(nx, ny, nz));
+  cudaStream_t st = ctx->stream;
+  const uint64_t nvox = (uint64_t)nx * ny * nz;
+  uint16_t* d_grid = nullptr;
+  cudaError_t ae = cudaMallocAsync(&d_grid, nvox * 2, st);
+  if (ae == cudaSuccess) ae = cudaMemcpyAsync(d_grid, h_grid, nvox * 2, cudaMemcpyHostToDevice, st);
+  if (ae != cudaSuccess) {
+    cudaFreeAsync(d_grid, st);
+    cudaStreamSynchronize(st);
+    return cuda_fail(ae, "dense scene: upload");
+  }
+  const meso_status rc = build_from_device_grid<uint16_t>(ctx, d_grid, nx, ny, nz, spare, st, out);
+  cudaFreeAsync(d_grid, st);
+  cudaStreamSynchronize(st);
+  return rc;
+}
+
+meso_status scene_create_grid(meso_ctx* ctx, int32_t kind, const void* d_grid, int32_t nx, int32_t ny, int32_t nz,
+                              uint64_t spare, meso_scene** out) {
+  if (!d_grid || !out) return fail(MESO_ERR_INVALID_ARG, "grid scene: null argument");
+  MESO_TRY(check_grid_dims(nx, ny, nz));
+  if (kind == MESO_SRC_GRID_U8)
+    return build_from_device_grid<uint8_t>(ctx, static_cast<const uint8_t*>(d_grid), nx, ny, nz, spare, ctx->stream,
+                                           out);
+  if (kind == MESO_SRC_GRID_U16)
+    return build_from_device_grid<uint16_t>(ctx, static_cast<const uint16_t*>(d_grid), nx, ny, nz, spare,
+                                            ctx->stream, out);
+  return fail(MESO_ERR_INVALID_ARG, "grid scene: kind must be MESO_SRC_GRID_U8 or MESO_SRC_GRID_U16");
+}
+
+meso_status scene_count_solid(meso_ctx* ctx, const meso_scene* s, uint64_t* n_solid) {
+  if (!s || !n_solid) return fail(MESO_ERR_INVALID_ARG, "scene_count_solid: null argument");
+  cudaStream_t st = ctx->stream;
+  unsigned long long* d = nullptr;
+  MESO_CUDA_TRY(cudaMallocAsync(&d, 8, st));
+  cudaError_t e = cudaMemsetAsync(d, 0, 8, st);
+  const uint64_t nb = n_bricks_of(s);
+  if (e == cudaSuccess) {
+    count_solid_kernel<<<(unsigned)std::min<uint64_t>((nb + 255) / 256, (uint64_t)ctx->sm_count * 16), 256, 0, st>>>(
+        s->d_ptr, nb, s->d_occ, d);
+    ctx->launches.fetch_add(1);
+    e = cudaGetLastError();
+  }
+  unsigned long long h = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(d, st);
+  const cudaError_t e2 = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return cuda_fail(e, "scene_count_solid");
+  *n_solid = h;
   return MESO_OK;
 }
 

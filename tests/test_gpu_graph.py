@@ -46,3 +46,34 @@ def test_graph_replay_mesh_and_raymarch(ctx):
         assert np.array_equal(hits.download(meso.HIT_DTYPE, ref_hits.shape[0], stream=st).view(np.uint8),
                               ref_hits.view(np.uint8))
     g.destroy()
+
+
+def test_graph_replay_raymarch_view_table(ctx):
+    """More than 32 views take the device view-table path (per-call table,
+    descriptors written by kernels whose parameters the graph keeps by
+    value); replays after the capturing call has returned give the direct
+    call's hits."""
+    L = meso.load()
+    st = ctx.stream()
+    scene = ctx.scene_from_terrain(meso.terrain_preset("small"))
+    rng = np.random.default_rng(11)
+    cams = [meso.camera((rng.uniform(-60, -20), rng.uniform(-60, 190), rng.uniform(60, 160)),
+                        (rng.uniform(30, 100), rng.uniform(30, 100), rng.uniform(0, 30)),
+                        int(rng.integers(8, 40)), int(rng.integers(8, 30))) for _ in range(70)]
+    ref = ctx.raymarch(scene, cams)
+    hits = ctx.alloc(ref.shape[0] * 24)
+    light = meso.light_dir()
+
+    def work():
+        sh = (ctypes.c_void_p * len(cams))(*([scene.handle] * len(cams)))
+        ca = (meso.Camera * len(cams))(*cams)
+        meso._check(L.meso_raymarch(ctx.handle, sh, ca, len(cams), light.ctypes.data, meso.RAY_SHADOW, hits.ptr, st))
+
+    g = ctx.capture(work, st)
+    for _ in range(2):
+        hits.zero(st)
+        g.launch(st)
+        ctx.sync(st)
+        assert np.array_equal(hits.download(meso.HIT_DTYPE, ref.shape[0], stream=st).view(np.uint8),
+                              ref.view(np.uint8))
+    g.destroy()

@@ -223,3 +223,55 @@ def test_matches_golden_fixture(ctx, small):
     hits = ctx.raymarch(scene, meso.camera((-40.0, -30.0, 140.0), (64.0, 64.0, 20.0), 96, 64))
     ref = np.load(os.path.join(golden, "hits_terrain128_96x64.npy"))
     assert np.array_equal(hits.view(np.uint8), ref.view(np.uint8))
+
+
+# The small plain case: the dense 256^3 uint8 value-noise grid (3 octaves,
+# seed 1), one 640x360 pinhole camera with a 60 degree vertical field of
+# view (the reference's default, Runtimes/Instance/VoxelWindowsInstance.h:22),
+# origin outside the grid aimed at its centre, marched to the first hit.
+CFG1_ORIGIN, CFG1_TARGET = (-160.0, -96.0, 384.0), (128.0, 128.0, 128.0)
+
+
+@pytest.fixture(scope="module")
+def dense256(ctx):
+    d = ctx.generate_dense_u8(256, 256, 256, seed=1)
+    host = oracle.gen_dense_u8(256, 256, 256, 1)
+    assert np.array_equal(d.download(np.uint8).reshape(256, 256, 256), host)
+    scene = ctx.scene_from_grid(meso.SRC_GRID_U8, d, (256, 256, 256))
+    bm = oracle.HostBrickMap.from_dense(host.astype(np.uint16))
+    return scene, bm, host
+
+
+def test_grid_u8_scene_build_bit_exact(dense256):
+    scene, bm, host = dense256
+    ptr, occ, mat = scene.download()
+    assert np.array_equal(ptr, bm.ptr())
+    assert np.array_equal(occ, bm.occ())
+    assert np.array_equal(mat, bm.mat())
+    assert np.array_equal(scene.dense(), host.astype(np.uint16))
+
+
+@pytest.mark.parametrize("shadow", [False, True])
+def test_raymarch_dense256_u8_640x360_matches_oracle(ctx, dense256, shadow):
+    scene, bm, _ = dense256
+    got = ctx.raymarch(scene, meso.camera(CFG1_ORIGIN, CFG1_TARGET, 640, 360), shadow=shadow)
+    ref = oracle.raymarch(bm, oracle.camera(CFG1_ORIGIN, CFG1_TARGET, 640, 360), shadow=shadow)
+    assert np.isfinite(ref["t"]).sum() > 640 * 360 // 4
+    assert_hits_equal(got, ref)
+
+
+def test_grid_u16_scene_equals_host_dense(ctx):
+    rng = np.random.default_rng(3)
+    g = ((rng.random((64, 96, 64)) < 0.1) * rng.integers(1, 65536, (64, 96, 64))).astype(np.uint16)
+    d = ctx.to_device(g)
+    a = ctx.scene_from_grid(meso.SRC_GRID_U16, d, (64, 96, 64))
+    b = ctx.scene_from_dense(g)
+    for x, y in zip(a.download(), b.download()):
+        assert np.array_equal(x, y)
+    with pytest.raises(meso.MesoError):
+        ctx.scene_from_grid(meso.SRC_CHUNKS_U16, d, (64, 96, 64))
+
+
+def test_scene_count_solid(ctx, small):
+    t, scene, bm = small
+    assert scene.count_solid() == int(np.count_nonzero(bm.dense()))
