@@ -256,7 +256,7 @@ def test_raymarch_dense256_u8_640x360_matches_oracle(ctx, dense256, shadow):
     scene, bm, _ = dense256
     got = ctx.raymarch(scene, meso.camera(CFG1_ORIGIN, CFG1_TARGET, 640, 360), shadow=shadow)
     ref = oracle.raymarch(bm, oracle.camera(CFG1_ORIGIN, CFG1_TARGET, 640, 360), shadow=shadow)
-    assert np.isfinite(ref["t"]).sum() > 640 * 360 // 4
+    assert np.isfinite(ref["t"]).sum() > 640 * 360 // 10  # the grid fills about a fifth of the frame
     assert_hits_equal(got, ref)
 
 
