@@ -67,6 +67,15 @@ def ncu_traffic(kernel):
         return None
 
 
+def ncu_field(kernel, key):
+    """A figure of one kernel from the committed ncu capture summary, or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_dram_bytes.json")) as f:
+            return json.load(f)[kernel][key]
+    except Exception:
+        return None
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -416,6 +425,55 @@ def bench_ray_dense256(ctx, meso, grid, steps, flush):
                              "kind": "port", "sample": f"the full 640x360 frame, {reps} runs of {cpu_s * 1e3:.1f} ms"}}
 
 
+def bench_mesh_brickmap(ctx, meso, scene, steps):
+    """Brick-map meshing: every 32^3 chunk of the 1024^3 terrain (32,768
+    chunks, neighbours' faces seen across chunk borders) in one persistent
+    launch, materials staged brick by brick (1 KiB bulk copies of the
+    occupied bricks).  Algorithmic bytes: 4 B per pointer fetched (64 per
+    chunk), 1 KiB of materials + 64 B of occupancy per occupied brick, the
+    one-voxel halo (6 x 32 x 32 occupancy bits per chunk) and 8 B per quad."""
+    import ctypes
+    L = meso._lib
+    n = 32 ** 3
+    idx = np.arange(n)
+    coords = ctx.to_device(np.stack([idx % 32, (idx // 32) % 32, idx // 1024], 1).astype(np.int32))
+    cap = 96 << 20
+    qbuf, cnt = ctx.alloc(cap * 8), ctx.alloc(8)
+    flush = ctx.alloc(L2_FLUSH_BYTES)
+    src = meso.MeshSource()
+    src.kind = meso.SRC_BRICKMAP
+    src.scene = scene.handle
+    out = meso.MeshOutput(qbuf.ptr, cap, cnt.ptr, None)
+
+    def run():
+        meso._check(L.meso_mesh_chunks(ctx.handle, ctypes.byref(src), coords.ptr, n, ctypes.byref(out), None))
+
+    for _ in range(3):
+        run()
+    evs = [(ctx.event(), ctx.event()) for _ in range(steps)]
+    for a, b in evs:
+        flush.zero()
+        ctx.record(a)
+        run()
+        ctx.record(b)
+    ctx.sync()
+    ms = sum(ctx.elapsed_ms(a, b) for a, b in evs) / steps
+    total = ctypes.c_uint64()
+    meso._check(L.meso_mesh_check(ctx.handle, ctypes.byref(out), None, ctypes.byref(total)))
+    quads = int(total.value)
+    bricks = int(scene.info().n_bricks)
+    algo = n * 64 * 4 + bricks * (1024 + 64) + n * 6 * 32 * 32 // 8 + 8 * quads
+    hbm = peaks()[0]
+    ach = algo / (ms * 1e6)
+    for b_ in (qbuf, cnt, flush, coords):
+        b_.free()
+    return {"workload": "all 32768 chunks of the 1024^3 terrain brick map (8^3 bricks, uint16), one persistent launch",
+            "gvox_s": round(n * 32768 / (ms * 1e6), 2), "ms": round(ms, 4), "quads": quads, "bricks": bricks,
+            "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(ach / hbm, 4), "algorithmic_bytes_per_launch": algo,
+                         "kernel": "mesh_kernel<BRICKMAP>"}}
+
+
 def cpu_mesh_baseline(m, n_single=512):
     """Oracle mesher on the host cores: all threads over the whole batched
     workload (checked bit for bit against the GPU's quads), one thread over
@@ -605,6 +663,57 @@ def bench_serve_render(ctx, meso, seconds, rate=2000.0):
     assert all(c.status == 0 for c in burst)
     res["workload"] = (f"4 resident scenes {dims}, Poisson {rate:.0f} req/s for {seconds:.0f} s (seed 7), "
                        "sizes {256^2, 512^2, 1920x1080, 3840x2160}, primary rays, HBM budget 120 GB")
+    # per image-size class: the class's requests among the first K, submitted
+    # at once (capacity) and one launch each, waited for (plain)
+    per_size, plain_s, cap_sz = {}, {}, {}
+    for w, h in sizes:
+        its = [it for it in items[:k] if (it[2].width, it[2].height) == (w, h)]
+        if not its:
+            continue
+        spx = len(its) * w * h
+        srv = meso.Server(ctx, scenes, max_inflight_batches=4, max_batch_rays=16 << 20, hbm_budget_bytes=120 << 30)
+        t0 = time.perf_counter()
+        for it in its:
+            srv.submit(it[1], it[2], shadow=False)
+        srv.drain(600.0)
+        cap_s = time.perf_counter() - t0
+        srv.poll(1 << 16)
+        srv.close()
+        ctx.sync()
+        t0 = time.perf_counter()
+        for it in its:
+            ctx.raymarch(scenes[it[1]], it[2], shadow=False, out=out, download=False)
+            ctx.sync()
+        plain_s[(w, h)] = time.perf_counter() - t0
+        cap_sz[(w, h)] = cap_s
+        per_size[f"{w}x{h}"] = {"requests": len(its), "capacity_mrays_s": round(spx / cap_s / 1e6, 1),
+                                "plain_per_view_mrays_s": round(spx / plain_s[(w, h)] / 1e6, 1),
+                                "capacity_over_plain": round(plain_s[(w, h)] / cap_s, 2)}
+    res["per_size"] = per_size
+    # the bound for this mix: even if batching made the two small classes cost
+    # nothing, the 1080p and 4K requests (whose single launches already fill
+    # the GPU) need at least their own batched time, so
+    # capacity/plain <= (plain time of all classes) / (batched time of the large classes)
+    big = sum(v for (w, h), v in cap_sz.items() if w * h >= 1920 * 1080)
+    res["mix_bound_capacity_over_plain"] = round(sum(plain_s.values()) / max(big, 1e-9), 2)
+    out.free()
+    # delivered: the same arrivals for half the time, each request's hits
+    # copied into page-locked host memory before its completion is reported
+    # (one destination buffer per size class, shared by the requests of that
+    # class: their contents are not read here)
+    dst = {wh: ctx.pinned(wh[0] * wh[1] * 24) for wh in sizes}
+    half = [it for it in items if it[0] <= seconds / 2]
+    srv = meso.Server(ctx, scenes, max_inflight_batches=4, max_batch_rays=16 << 20, max_queue=512,
+                      hbm_budget_bytes=120 << 30)
+    comps = replay(srv, half, lambda it: srv.submit(it[1], it[2], shadow=False,
+                                                    dst=dst[(it[2].width, it[2].height)]))
+    srv.close()
+    d = summarize(comps)
+    d["workload"] = f"the first {seconds / 2:.0f} s of the same arrivals, hits delivered into page-locked host memory"
+    d["delivered_gb_s"] = round(sum(c.n_rays for c in comps if c.status == 0) * 24 / d["span_s"] / 1e9, 1)
+    res["delivered"] = d
+    for b_ in dst.values():
+        b_.free()
     for s in scenes:
         s.destroy()
     return res
@@ -629,11 +738,18 @@ def bench_serve_edit(ctx, meso, seconds, rate=200.0):
             edits.append(meso.SphereEdit((ctypes.c_int32 * 3)(*c), int(rng.integers(2, 33)), m, 0))
         o, tg = outside_pose(rng, n, (edits[0].center[0], edits[0].center[1], edits[0].center[2]))
         items.append((ta, edits, meso.camera(o, tg, 1920, 1080)))
+    # the server keeps the scene's mesh store current and delivers each render
+    # into page-locked host memory before reporting it complete
+    dst = ctx.pinned(1920 * 1080 * 24)
     srv = meso.Server(ctx, [scene], max_inflight_batches=4, max_batch_rays=4 << 20, max_queue=512,
-                      max_edit_quads=64 << 20)
-    comps = replay(srv, items, lambda it: srv.submit(0, it[2], shadow=False, edits=it[1]))
+                      max_edit_quads=64 << 20, keep_meshes=1)
+    comps = replay(srv, items, lambda it: srv.submit(0, it[2], shadow=False, edits=it[1], dst=dst))
+    si = srv.store(0).info()
+    store_info = {"live_quads": int(si.live_quads), "arena_quads": int(si.arena_quads),
+                  "arena_used": int(si.arena_used), "compactions": int(si.compactions)}
     srv.close()
     res = summarize(comps)
+    res["mesh_store"] = store_info
     ok = [c for c in comps if c.status == 0]
     chunks = sum(c.n_dirty_chunks for c in ok)
     busy = sum(c.done_s - c.start_s for c in ok)
@@ -642,17 +758,19 @@ def bench_serve_edit(ctx, meso, seconds, rate=200.0):
     res["gvox_meshed_s_wall"] = round(chunks * 32768 / res["span_s"] / 1e9, 3)
     res["gvox_meshed_s_busy"] = round(chunks * 32768 / max(busy, 1e-9) / 1e9, 3)
     res["workload"] = (f"4096^3 terrain (512^3 pointer grid), Poisson {rate:.0f} req/s for {seconds:.0f} s (seed 9), "
-                       "1-32 sphere edits + remesh of dirty chunks + 1920x1080 primary render")
+                       "1-32 sphere edits + remesh of dirty chunks into the scene's resident mesh store + "
+                       "1920x1080 primary render delivered into page-locked host memory")
     res["voxel_occupancy"] = round(occupancy, 5)
     # capacity (requests submitted at once) and the plain form (edit, one mesh
     # launch per dirty chunk, one render launch, waited for) on fresh copies
     k = min(200, len(items))
     scene.destroy()
     scene = ctx.scene_from_terrain(t, spare_bricks=4 << 20)
-    srv = meso.Server(ctx, [scene], max_inflight_batches=4, max_batch_rays=4 << 20, max_edit_quads=64 << 20)
+    srv = meso.Server(ctx, [scene], max_inflight_batches=4, max_batch_rays=4 << 20, max_edit_quads=64 << 20,
+                      keep_meshes=1)
     t0 = time.perf_counter()
     for it in items[:k]:
-        srv.submit(0, it[2], shadow=False, edits=it[1])
+        srv.submit(0, it[2], shadow=False, edits=it[1], dst=dst)
     srv.drain(600.0)
     cap_s = time.perf_counter() - t0
     comps = srv.poll(1 << 16)
@@ -681,6 +799,7 @@ def bench_serve_edit(ctx, meso, seconds, rate=200.0):
                                                       ctypes.byref(mo), None))
             plain_chunks += len(dirty)
         ctx.raymarch(scene, it[2], shadow=False, out=hits, download=False)
+        meso._check(L.meso_memcpy_d2h(ctx.handle, dst.ptr, hits.ptr, 1920 * 1080 * 24, None))
         ctx.sync()
     plain_s = time.perf_counter() - t0
     res["capacity_requests"] = k
@@ -760,6 +879,11 @@ def run_ours(args, world, rank, local, dist):
             "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
             "frac": round(achieved / hbm, 4), "traffic": ncu_traffic("raymarch_kernel"), "peak_source": which,
             "kernel": "raymarch_kernel",
+            # what limits it (ncu): instruction issue, not DRAM -- its fetches hit in L1/L2
+            "limiter": "issue",
+            "issue_active_pct": ncu_field("raymarch_kernel", "smsp__issue_active_pct"),
+            "active_lanes_per_instruction": ncu_field("raymarch_kernel", "active_lanes_per_instruction"),
+            "l2_frac": round(achieved / l2, 4),
             "l2": {"peak": round(l2, 1), "unit": "GB/s", "frac": round(achieved / l2, 4),
                    "how": "meso_measure_l2_read: a 32 MiB buffer read 50 times with 16-byte L1-bypassing loads"},
             "algorithmic_bytes_per_launch": int(r["algo_bytes"]),
@@ -782,6 +906,7 @@ def run_ours(args, world, rank, local, dist):
         if not args.skip_cpu:
             line["mesh"]["cpu_baseline"] = cpu_mesh_baseline(m)
         line["mesh"]["uint8"] = bench_mesh_u8(ctx, meso, m, args.steps)
+        line["mesh"]["brickmap"] = bench_mesh_brickmap(ctx, meso, r["scene"], args.steps)
         line["downstream"] = bench_downstream(ctx, meso, m, args.steps)
     if rank == 0 and not args.skip_serve:
         line["served"] = bench_serve_render(ctx, meso, args.serve_seconds)

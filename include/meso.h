@@ -316,6 +316,47 @@ meso_status meso_raymarch_noalloc(meso_ctx* ctx, const meso_scene* const* scenes
                                   uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
                                   void* stream);
 
+/* ------------------------------------------------------------- mesh store */
+
+/* The resident mesh of a brick-map scene: every chunk's quads in one device
+ * arena, found through a per-chunk segment table, and replaced chunk by chunk
+ * when edits dirty them.  Stands in for the reference's pooled chunk output:
+ * slot allocation and replacement in FChunkPool::PushToPool
+ * (Runtimes/Voxel/Chunk/ChunkPool.h:446-622), the per-chunk block instances
+ * written by PushToBlockPool (:381-445) and their upload for drawing
+ * (:653-679).  Quads in the arena are the packed format above with the chunk
+ * field cleared (the segment names the chunk); their order inside a segment
+ * is unspecified.  A store reads its scene, which must outlive it. */
+typedef struct meso_mesh_store meso_mesh_store;
+
+typedef struct meso_mesh_store_info {
+  uint64_t n_chunks;             /* (nx/32)(ny/32)(nz/32), chunk c = x + CX*(y + CY*z) */
+  uint64_t live_quads;           /* quads held in all segments */
+  uint64_t arena_quads;          /* arena capacity */
+  uint64_t arena_used;           /* bump pointer: segments (with slack) + replaced ones */
+  uint64_t compactions;          /* times the arena was repacked */
+  const uint64_t* d_arena;       /* device arena */
+  const uint64_t* d_seg_offset;  /* per chunk: first quad (UINT64_MAX: none) */
+  const uint32_t* d_seg_count;   /* per chunk: quads */
+} meso_mesh_store_info;
+
+/* Meshes every non-empty chunk of the scene into a new store (waits). */
+meso_status meso_mesh_store_create(meso_ctx* ctx, const meso_scene* scene, meso_mesh_store** out);
+/* Remeshes the n listed chunks (linear indices, e.g. the dirty list of
+ * meso_edit_spheres) in one batched launch and replaces their segments: in
+ * place when the new quads fit, else at the arena's end; a full arena is
+ * repacked (and grown) before the update completes.  Returns when the store
+ * holds the new segments. */
+meso_status meso_mesh_store_update(meso_ctx* ctx, meso_mesh_store* store, const uint32_t* h_chunks, uint32_t n);
+meso_status meso_mesh_store_get_info(meso_ctx* ctx, const meso_mesh_store* store, meso_mesh_store_info* info);
+/* Copies the segments of the n listed chunks (at most 2^20) into d_out in
+ * list order; quads of the k-th listed chunk carry chunk field k.
+ * *h_total receives the number of quads (MESO_ERR_OVERFLOW when it exceeds
+ * capacity).  Waits for the copy. */
+meso_status meso_mesh_store_gather(meso_ctx* ctx, const meso_mesh_store* store, const uint32_t* h_chunks, uint32_t n,
+                                   uint64_t* d_out, uint64_t capacity, uint64_t* h_total);
+meso_status meso_mesh_store_destroy(meso_ctx* ctx, meso_mesh_store* store);
+
 /* ------------------------------------------------------------------- edits */
 
 typedef struct meso_sphere_edit {
@@ -350,6 +391,9 @@ typedef struct meso_request {
   uint32_t n_edits;
   const meso_sphere_edit* edits; /* copied at submit */
   uint64_t user_tag;
+  meso_hit* dst_hits;       /* optional caller-owned destination of the request's
+                               width*height hits: device memory or page-locked host
+                               memory; the completion is reported after they land */
 } meso_request;
 
 typedef struct meso_completion {
@@ -373,6 +417,9 @@ typedef struct meso_server_config {
   uint32_t max_queue;             /* queued requests beyond this are rejected, 0 = no bound */
   float light[3];                 /* direction towards the light (0,0,0 = normalize(0.3,0.5,0.8)) */
   uint64_t max_edit_quads;        /* quad buffer of a remesh, 0 = 16M */
+  uint32_t keep_meshes;           /* 1 = keep a mesh store per scene (created at server
+                                     creation), updated by every edit request's remesh */
+  uint32_t reserved;
 } meso_server_config;
 
 /* The serving loop replaces the host ThreadPool + TDoubleBufferQueue pair
@@ -386,6 +433,10 @@ meso_status meso_server_submit(meso_server* srv, const meso_request* req, uint64
 meso_status meso_server_poll(meso_server* srv, meso_completion* out, uint32_t max, uint32_t* n);
 /* Copies the hits of a finished request (keep_hits = 1) and releases them. */
 meso_status meso_server_fetch_hits(meso_server* srv, uint64_t request_id, meso_hit* h_hits, uint64_t capacity);
+/* The mesh store the server keeps for scene scene_index (keep_meshes = 1);
+ * owned by the server.  Read it only while no edit of that scene is in
+ * flight (e.g. after meso_server_drain). */
+meso_status meso_server_get_store(meso_server* srv, uint32_t scene_index, meso_mesh_store** out);
 meso_status meso_server_drain(meso_server* srv, double timeout_s);
 double meso_server_now(const meso_server* srv);
 meso_status meso_server_destroy(meso_server* srv);

@@ -82,6 +82,14 @@ class MeshOutput(ctypes.Structure):
     ]
 
 
+class MeshStoreInfo(ctypes.Structure):
+    _fields_ = [
+        ("n_chunks", ctypes.c_uint64), ("live_quads", ctypes.c_uint64), ("arena_quads", ctypes.c_uint64),
+        ("arena_used", ctypes.c_uint64), ("compactions", ctypes.c_uint64), ("d_arena", ctypes.c_void_p),
+        ("d_seg_offset", ctypes.c_void_p), ("d_seg_count", ctypes.c_void_p),
+    ]
+
+
 class Camera(ctypes.Structure):
     _fields_ = [
         ("origin_chunk", ctypes.c_int32 * 3), ("origin_frac", ctypes.c_float * 3),
@@ -99,6 +107,7 @@ class Request(ctypes.Structure):
     _fields_ = [
         ("kind", ctypes.c_uint32), ("scene_index", ctypes.c_uint32), ("camera", Camera), ("flags", ctypes.c_uint32),
         ("n_edits", ctypes.c_uint32), ("edits", ctypes.POINTER(SphereEdit)), ("user_tag", ctypes.c_uint64),
+        ("dst_hits", ctypes.c_void_p),
     ]
 
 
@@ -116,6 +125,7 @@ class ServerConfig(ctypes.Structure):
         ("max_inflight_batches", ctypes.c_uint32), ("max_batch_requests", ctypes.c_uint32),
         ("max_batch_rays", ctypes.c_uint64), ("hbm_budget_bytes", ctypes.c_uint64), ("keep_hits", ctypes.c_uint32),
         ("max_queue", ctypes.c_uint32), ("light", ctypes.c_float * 3), ("max_edit_quads", ctypes.c_uint64),
+        ("keep_meshes", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
     ]
 
 
@@ -154,6 +164,12 @@ _SIGNATURES = {
                                ctypes.c_int32, ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)],
     "meso_scene_count_solid": [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)],
     "meso_scene_destroy": [ctypes.c_void_p, ctypes.c_void_p],
+    "meso_mesh_store_create": [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)],
+    "meso_mesh_store_update": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32],
+    "meso_mesh_store_get_info": [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(MeshStoreInfo)],
+    "meso_mesh_store_gather": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                               ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
+    "meso_mesh_store_destroy": [ctypes.c_void_p, ctypes.c_void_p],
     "meso_scene_get_info": [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(SceneInfo)],
     "meso_scene_download": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     "meso_generate_dense_u8": [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint32,
@@ -186,6 +202,7 @@ _SIGNATURES = {
                          ctypes.POINTER(ctypes.c_uint32)],
     "meso_server_fetch_hits": [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64],
     "meso_server_drain": [ctypes.c_void_p, ctypes.c_double],
+    "meso_server_get_store": [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)],
     "meso_server_destroy": [ctypes.c_void_p],
     "meso_autotune": [ctypes.c_void_p, ctypes.c_char_p],
     "meso_scene_save": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p],
@@ -372,6 +389,60 @@ class Scene:
     def destroy(self) -> None:
         if self.handle and _lib is not None:
             _lib.meso_scene_destroy(self.ctx.handle, self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class MeshStore:
+    """The resident per-chunk mesh of a brick-map scene (meso_mesh_store)."""
+
+    def __init__(self, ctx: "Context", scene: "Scene", handle=None):
+        self.ctx = ctx
+        self.scene = scene  # the store reads the scene: keep it alive
+        self.owned = handle is None
+        if handle is None:
+            h = ctypes.c_void_p()
+            _check(_lib.meso_mesh_store_create(ctx.handle, scene.handle, ctypes.byref(h)))
+            handle = h.value
+        self.handle = handle
+
+    @classmethod
+    def borrowed(cls, ctx: "Context", scene: "Scene", handle: int) -> "MeshStore":
+        return cls(ctx, scene, handle)
+
+    def update(self, chunks) -> None:
+        c = np.ascontiguousarray(chunks, dtype=np.uint32)
+        _check(_lib.meso_mesh_store_update(self.ctx.handle, self.handle, _np_ptr(c), c.size))
+
+    def info(self) -> MeshStoreInfo:
+        i = MeshStoreInfo()
+        _check(_lib.meso_mesh_store_get_info(self.ctx.handle, self.handle, ctypes.byref(i)))
+        return i
+
+    def gather(self, chunks) -> np.ndarray:
+        """Quads of the listed chunks in list order (chunk field = position in the list)."""
+        c = np.ascontiguousarray(chunks, dtype=np.uint32)
+        total = ctypes.c_uint64()
+        # a size query: with capacity 0 the call reports the total (and
+        # MESO_ERR_OVERFLOW when it is not zero)
+        rc = _lib.meso_mesh_store_gather(self.ctx.handle, self.handle, _np_ptr(c), c.size, None, 0,
+                                         ctypes.byref(total))
+        if rc not in (0, 4):
+            _check(rc)
+        n = int(total.value)
+        out = self.ctx.alloc(max(8, n * 8))
+        _check(_lib.meso_mesh_store_gather(self.ctx.handle, self.handle, _np_ptr(c), c.size, out.ptr, n,
+                                           ctypes.byref(total)))
+        return out.download(np.uint64, n)
+
+    def destroy(self) -> None:
+        if self.handle and self.owned:
+            _lib.meso_mesh_store_destroy(self.ctx.handle, self.handle)
         self.handle = None
 
     def __del__(self):
@@ -625,6 +696,9 @@ class Context:
         _check(_lib.meso_measure_l2_read(self.handle, nbytes, passes, ctypes.byref(g)))
         return g.value
 
+    def mesh_store(self, scene: Scene) -> MeshStore:
+        return MeshStore(self, scene)
+
     def autotune(self, path: str | None = None) -> None:
         _check(_lib.meso_autotune(self.handle, path.encode() if path else None))
 
@@ -756,8 +830,11 @@ class Server:
         self.handle = h.value
         self._keep = {}
 
-    def submit(self, scene_index: int, camera: Camera, shadow=False, edits=None, tag=0) -> int:
+    def submit(self, scene_index: int, camera: Camera, shadow=False, edits=None, tag=0, dst=None) -> int:
+        """dst: optional DeviceBuffer / PinnedBuffer (or raw pointer) that receives the request's hits."""
         r = Request()
+        if dst is not None:
+            r.dst_hits = dst if isinstance(dst, int) else dst.ptr
         r.kind = REQ_EDIT_REMESH_RENDER if edits is not None else REQ_RENDER
         r.scene_index = scene_index
         r.camera = camera
@@ -771,6 +848,12 @@ class Server:
         rid = ctypes.c_uint64()
         _check(_lib.meso_server_submit(self.handle, ctypes.byref(r), ctypes.byref(rid)))
         return int(rid.value)
+
+    def store(self, scene_index: int) -> "MeshStore":
+        """The mesh store the server keeps for a scene (keep_meshes=1); owned by the server."""
+        h = ctypes.c_void_p()
+        _check(_lib.meso_server_get_store(self.handle, scene_index, ctypes.byref(h)))
+        return MeshStore.borrowed(self.ctx, self.scenes[scene_index], h.value)
 
     def poll(self, max_n: int = 4096):
         buf = (Completion * max_n)()

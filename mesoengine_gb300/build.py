@@ -17,8 +17,12 @@ OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libmeso_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math",
-         "-Xcompiler", "-Wall,-Wno-unused-function", "-I", os.path.join(ROOT, "include")]
+# nvcc warnings are errors: a host-only call from device code (a "calling a
+# __host__ function from a __host__ __device__ function" warning) compiles to
+# undefined device code otherwise.
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Werror", "all-warnings", "-Xcompiler",
+         "-fPIC,-ffp-contract=off,-fno-fast-math", "-Xcompiler", "-Wall,-Wno-unused-function",
+         "-I", os.path.join(ROOT, "include")]
 
 
 def _sources():

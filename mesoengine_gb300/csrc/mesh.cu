@@ -287,8 +287,11 @@ __device__ __forceinline__ void issue_chunk(MeshSmem& sm, uint8_t* dst, const Me
       if (lane == 0) {
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(bar, n_full * 1024u);
+        // no occupied brick: no solid voxel, so no face and nothing to stage
+        if (n_full == 0) sm.valid = 2;
       }
       __syncwarp();
+      if (n_full == 0) return;
       for (int k = 0; k < 2; k++) {
         const int b = lane + 32 * k;
         uint8_t* d = dst + b * kBrickSlot;
@@ -433,6 +436,20 @@ __device__ __forceinline__ uint32_t isolated(uint32_t f, uint32_t fu, uint32_t f
   return f & ~(left | (left >> 1) | (f & vv & fu) | (f & vd & fd));
 }
 
+// Position of the (r+1)-th set bit of w (r < popc(w)): halving on popcounts.
+__device__ __forceinline__ uint32_t select_bit(uint32_t w, uint32_t r) {
+  uint32_t pos = 0, c;
+  c = __popc(w & 0xFFFFu);
+  if (r >= c) { r -= c; w >>= 16; pos = 16; }
+  c = __popc(w & 0xFFu);
+  if (r >= c) { r -= c; w >>= 8; pos += 8; }
+  c = __popc(w & 0xFu);
+  if (r >= c) { r -= c; w >>= 4; pos += 4; }
+  c = __popc(w & 0x3u);
+  if (r >= c) { r -= c; w >>= 2; pos += 2; }
+  return pos + (r >= (w & 1u) ? 1u : 0u);
+}
+
 // Appends the warp's staged quads to the output (one atomic per flush).
 __device__ __forceinline__ void flush_warp(MeshSmem& sm, int warp, const MeshParams& p, int lane, uint32_t cnt) {
   __syncwarp();
@@ -514,7 +531,8 @@ __global__ void __launch_bounds__(kThreads, KindTraits<KIND>::kCtasPerSm)
     __syncthreads();
     const int c = sm.chunk;
     if (c < 0) break;
-    const bool valid = sm.valid != 0;
+    // valid: 1 = mesh it; 0 = bad coordinate (flagged); 2 = no occupied brick
+    const bool valid = sm.valid == 1;
     if constexpr (T::kHalo) {
       if (valid) compute_halos<KIND>(sm, p, warp, lane);
     }
@@ -634,10 +652,13 @@ __global__ void __launch_bounds__(kThreads, KindTraits<KIND>::kCtasPerSm)
         __syncthreads();
         // ---- pass 3: isolated quads of this warp's words, the 4 rows of one
         // direction at a time (lane = slice).  A warp-balanced expansion over
-        // all set bits of the 4 x 32 words: lane j of round k emits the
-        // (32k+j)-th bit, found by a shuffle binary search over the lanes'
-        // prefixes, then the row from the owning lane's packed running
-        // counts, then __fns inside that word.
+        // all set bits of the 4 x 32 words: lane j of a round takes the
+        // (32k+j)-th bit; its owning lane comes from a binary search over
+        // the lanes' exclusive prefixes, the row from the owner's packed
+        // running counts, the word from the warp's staging buffer (its
+        // greedy staging area, empty at this point), the column from a
+        // popcount-halving select.
+        uint32_t* const stage = reinterpret_cast<uint32_t*>(sm.qbuf[warp]);  // [row q][lane]
 #pragma unroll 1
         for (int dir = dbase; dir < dbase + 3; dir++) {
           // this direction's words are isow[0..3]; the rest shift down by 4
@@ -655,32 +676,36 @@ __global__ void __launch_bounds__(kThreads, KindTraits<KIND>::kCtasPerSm)
           const uint32_t G = __shfl_sync(kFull, incl, 31);
           if (G == 0) continue;
           const uint32_t ex = incl - n;
-          const uint32_t packed = c1 | c2 << 8 | c3 << 16;  // running counts, each <= 96
+          // running counts before rows 1, 2, 3 in bytes 1..3 (byte 0: 0)
+          const uint32_t packed = c1 << 8 | c2 << 16 | c3 << 24;
+          stage[lane] = w0;
+          stage[32 + lane] = w1;
+          stage[64 + lane] = w2;
+          stage[96 + lane] = w3;
+          __syncwarp();
+          // run: this direction's first output index (the warp reserved all
+          // three directions' isolated quads at once, after pass 2)
+          const bool all_fit = run + G <= p.cap;
+          uint2* const dst = reinterpret_cast<uint2*>(p.quads) + run;
           // bit offsets of slice, column and row in the linear voxel index
           const int sh_s = dir < 2 ? 0 : (dir < 4 ? 5 : 10);
           const int sh_u = dir < 2 ? 5 : 0;
           const int sh_v = dir < 4 ? 10 : 5;
-          const uint64_t dir_bits = chunk_bits | (uint64_t)dir << 41;
-          // two rounds (64 bits) per pass, so their shuffle chains interleave
+          const uint32_t hi_bits = (uint32_t)(chunk_bits >> 32) | (uint32_t)dir << 9;
           auto emit = [&](uint32_t j, int l) {
             const uint32_t r = j - __shfl_sync(kFull, ex, l);
             const uint32_t pk = __shfl_sync(kFull, packed, l);
-            const uint32_t x0 = __shfl_sync(kFull, w0, l), x1 = __shfl_sync(kFull, w1, l);
-            const uint32_t x2 = __shfl_sync(kFull, w2, l), x3 = __shfl_sync(kFull, w3, l);
             if (j < G) {
-              const uint32_t p1 = pk & 0xFFu, p2 = (pk >> 8) & 0xFFu, p3 = pk >> 16;
-              uint32_t wq = x0, rb = 0;
-              int q = 0;
-              if (r >= p1) { wq = x1; rb = p1; q = 1; }
-              if (r >= p2) { wq = x2; rb = p2; q = 2; }
-              if (r >= p3) { wq = x3; rb = p3; q = 3; }
-              const uint32_t u = __fns(wq, 0, (int)(r - rb) + 1);
-              const uint32_t lin = (uint32_t)l << sh_s | u << sh_u | (uint32_t)(v0 + q) << sh_v;
+              const uint32_t q = (uint32_t)(r >= ((pk >> 8) & 0xFFu)) + (uint32_t)(r >= ((pk >> 16) & 0xFFu)) +
+                                 (uint32_t)(r >= (pk >> 24));
+              const uint32_t rb = (pk >> (8 * q)) & 0xFFu;
+              const uint32_t u = select_bit(stage[32 * q + l], r - rb);
+              const uint32_t lin = (uint32_t)l << sh_s | u << sh_u | ((uint32_t)v0 + q) << sh_v;
               const uint32_t mat = load_mat_lin<KIND>(mb, lin);
-              const unsigned long long idx = run + j;
-              if (idx < p.cap) p.quads[idx] = dir_bits | (uint64_t)lin << 26 | mat;
+              if (all_fit || run + j < p.cap) dst[j] = make_uint2(lin << 26 | mat, hi_bits | lin >> 6);
             }
           };
+          // two rounds (64 bits) per pass, so their shuffle chains interleave
           for (uint32_t k2 = 0; k2 < G; k2 += 64) {
             const uint32_t ja = k2 + (uint32_t)lane, jb = ja + 32u;
             int la = 0, lb = 0;
@@ -695,6 +720,7 @@ __global__ void __launch_bounds__(kThreads, KindTraits<KIND>::kCtasPerSm)
             if (k2 + 32u < G) emit(jb, lb);
           }
           run += G;
+          __syncwarp();  // the stage is rewritten by the next direction
         }
         // ---- pass 4: greedy on the remaining faces, one warp per slice.
         // Lane r holds row r of the slice in registers: its faces (isolated
@@ -728,7 +754,7 @@ __global__ void __launch_bounds__(kThreads, KindTraits<KIND>::kCtasPerSm)
               smask = rs[d];
             }
           }
-          const int sl = (int)__fns(smask, 0, (int)(t - before) + 1);
+          const int sl = (int)select_bit(smask, t - before);
           const int orow = word_off(dir, sl, lane);
           const uint32_t F0 = face_col(sm, dir, sl, lane);
           const uint32_t Er = e_arr(sm, dir)[orow];
@@ -826,6 +852,10 @@ __global__ void __launch_bounds__(kThreads, KindTraits<KIND>::kCtasPerSm)
           }
         }
         if (p.chunk_counts && lane == 0 && mine) atomicAdd(&sm.chunk_quads, mine);
+        if (qc) {  // the staging area doubles as pass 3's word buffer
+          flush_warp(sm, warp, p, lane, qc);
+          qc = 0;
+        }
       }
     }
     __syncthreads();

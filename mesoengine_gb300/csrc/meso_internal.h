@@ -130,6 +130,21 @@ meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, cons
                             uint64_t* d_stats = nullptr);
 size_t raymarch_view_table_bytes(uint32_t n_views);
 
+// Mesh store internals shared with the serving loop (store.cu).
+// Places the quads of the n chunks at d_coords that a batched mesh launch
+// left in d_temp (counts per chunk in d_counts) into the store's segments;
+// stream-ordered.  d_work holds 12 * n bytes.
+meso_status store_place_async(meso_ctx* ctx, meso_mesh_store* S, const int32_t* d_coords, uint32_t n,
+                              const uint64_t* d_temp, uint64_t temp_cap, const unsigned long long* d_temp_count,
+                              const uint32_t* d_counts, void* d_work, cudaStream_t st);
+// Remeshes the listed chunks (linear indices) and waits until the store holds them.
+meso_status store_update_sync(meso_ctx* ctx, meso_mesh_store* S, const uint32_t* h_chunks, uint32_t n,
+                              cudaStream_t st);
+// Device word of the store's flags (nonzero: a placement failed and the
+// chunks of that update must be placed again with store_update_sync).
+unsigned long long* store_flags_word(meso_mesh_store* S);
+uint64_t store_device_bytes(const meso_mesh_store* S);
+
 }  // namespace meso
 
 // ------------------------------------------------------------ PTX wrappers

@@ -125,6 +125,11 @@ struct Slot {
   int32_t* d_coords = nullptr;
   int32_t* h_coords = nullptr;  // pinned staging
   uint32_t coord_cap = 0;
+  // keep_meshes: per-chunk quad counts of the remesh, placement scratch
+  // (12 bytes per chunk) and the store's flags copied back with the results
+  uint32_t* d_counts = nullptr;
+  void* d_place = nullptr;
+  unsigned long long* h_flags = nullptr;
   meso_hit* h_hits = nullptr;  // pinned, keep_hits only
   bool busy = false;
   bool edit = false;
@@ -159,6 +164,7 @@ struct meso_server {
   uint64_t inflight = 0;
   std::chrono::steady_clock::time_point t0;
   std::vector<uint32_t> dirty;  // scratch for edit dirty lists
+  std::vector<meso_mesh_store*> stores;  // keep_meshes: one per scene
   double now() const {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   }
@@ -174,6 +180,9 @@ void release_slot(Slot& s) {
   cudaFree(s.d_sums);
   cudaFree(s.d_quads);
   cudaFree(s.d_coords);
+  cudaFree(s.d_counts);
+  cudaFree(s.d_place);
+  cudaFreeHost(s.h_flags);
   cudaFreeHost(s.h_sums);
   cudaFreeHost(s.h_coords);
   cudaFreeHost(s.h_hits);
@@ -291,10 +300,21 @@ void launch_batch(meso_server* srv, Slot& s) {
       o.d_quads = s.d_quads;
       o.capacity = s.quad_cap;
       o.d_quad_count = reinterpret_cast<uint64_t*>(s.d_sums + 2 * kMaxBatch + 1);
-      o.d_chunk_quad_counts = nullptr;
+      meso_mesh_store* store = srv->stores.empty() ? nullptr : srv->stores[r.req.scene_index];
+      o.d_chunk_quad_counts = store ? s.d_counts : nullptr;
       rc = launch_mesh(ctx, &src, s.d_coords, n_dirty, &o, st, false);
       if (rc == MESO_OK)
         quad_hash_kernel<<<64, 256, 0, st>>>(s.d_quads, o.d_quad_count, s.quad_cap, s.d_sums + 2 * kMaxBatch);
+      // the scene's resident mesh: the dirty chunks' new quads replace their
+      // segments; a failed placement is flagged and repaired at completion
+      if (rc == MESO_OK && store)
+        rc = store_place_async(ctx, store, s.d_coords, n_dirty, s.d_quads, s.quad_cap,
+                               reinterpret_cast<const unsigned long long*>(o.d_quad_count), s.d_counts, s.d_place,
+                               st);
+      if (rc == MESO_OK && store) {
+        cudaMemcpyAsync(s.h_flags, store_flags_word(store), sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+        cudaMemsetAsync(store_flags_word(store), 0, sizeof(unsigned long long), st);
+      }
     }
     s.n_dirty = n_dirty;
   }
@@ -308,6 +328,11 @@ void launch_batch(meso_server* srv, Slot& s) {
     dim3 grid(std::min<uint32_t>(per_seg, 1024u), segs.n);
     hit_hash_kernel<<<grid, 256, 0, rs>>>(reinterpret_cast<const uint64_t*>(s.d_hits), segs, s.d_sums);
     ctx->launches.fetch_add(s.edit ? 2 : 1);
+    // delivery into the callers' buffers, before the completion is signalled
+    for (size_t k = 0; k < s.reqs.size(); k++) {
+      meso_hit* dst = s.reqs[k].req.dst_hits;
+      if (dst) cudaMemcpyAsync(dst, s.d_hits + s.offsets[k], s.reqs[k].pixels * sizeof(meso_hit), cudaMemcpyDefault, rs);
+    }
     if (s.edit) {
       cudaEventRecord(s.joined, rs);
       cudaStreamWaitEvent(st, s.joined, 0);
@@ -315,11 +340,32 @@ void launch_batch(meso_server* srv, Slot& s) {
     cudaMemcpyAsync(s.h_sums, s.d_sums, sizeof(unsigned long long) * (2 * kMaxBatch + 2), cudaMemcpyDeviceToHost, st);
     if (srv->cfg.keep_hits) cudaMemcpyAsync(s.h_hits, s.d_hits, off * sizeof(meso_hit), cudaMemcpyDeviceToHost, st);
   }
+  if (rc == MESO_OK) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = cuda_fail(e, "server: batch launch");
+  }
   s.launch_status = rc;
   cudaEventRecord(s.done, st);
 }
 
+// A remesh whose placement in the scene's mesh store failed (full arena or
+// temporary buffer) is placed again, synchronously, before the scene's next
+// request may start.
+meso_status repair_store(meso_server* srv, Slot& s) {
+  meso_mesh_store* store = srv->stores[s.reqs[0].req.scene_index];
+  const meso_scene* scene = srv->scenes[s.reqs[0].req.scene_index];
+  const uint32_t CX = (uint32_t)scene->nx / 32, CY = (uint32_t)scene->ny / 32;
+  std::vector<uint32_t> chunks(s.n_dirty);
+  for (uint32_t k = 0; k < s.n_dirty; k++)
+    chunks[k] = (uint32_t)s.h_coords[3 * k] + CX * ((uint32_t)s.h_coords[3 * k + 1] + CY * (uint32_t)s.h_coords[3 * k + 2]);
+  return store_update_sync(srv->ctx, store, chunks.data(), s.n_dirty, s.stream);
+}
+
 void finish_batch(meso_server* srv, Slot& s) {
+  if (s.edit && s.launch_status == MESO_OK && !srv->stores.empty() && s.n_dirty && *s.h_flags) {
+    *s.h_flags = 0;
+    s.launch_status = repair_store(srv, s);
+  }
   std::vector<meso_completion> comps;
   for (size_t k = 0; k < s.reqs.size(); k++) {
     const SrvRequest& r = s.reqs[k];
@@ -434,16 +480,32 @@ meso_status meso_server_create(meso_ctx* ctx, const meso_server_config* cfg, mes
     max_chunks = std::max<uint32_t>(max_chunks, (uint32_t)((scenes[i]->nx / 32) * (scenes[i]->ny / 32) *
                                                            (uint64_t)(scenes[i]->nz / 32)));
   }
+  if (srv->cfg.keep_meshes) {
+    for (uint32_t i = 0; i < n_scenes; i++) {
+      meso_mesh_store* st = nullptr;
+      const meso_status rc = meso_mesh_store_create(ctx, scenes[i], &st);
+      if (rc != MESO_OK) {
+        for (meso_mesh_store* t : srv->stores) meso_mesh_store_destroy(ctx, t);
+        delete srv;
+        return rc;
+      }
+      srv->stores.push_back(st);
+    }
+  }
+  uint64_t store_bytes = 0;
+  for (meso_mesh_store* t : srv->stores) store_bytes += store_device_bytes(t);
   srv->scene_busy.assign(n_scenes, 0);
   srv->scene_edit_busy.assign(n_scenes, 0);
   srv->dirty.assign(std::max<uint32_t>(max_chunks, 1), 0);
   // per slot: hits, view table, sums, quads, coordinates
   const uint32_t coord_cap = std::min<uint32_t>(max_chunks, MESO_MAX_CHUNKS_PER_CALL);
   const uint64_t per_slot = srv->cfg.max_batch_rays * sizeof(meso_hit) + raymarch_view_table_bytes(kMaxBatch) +
-                            srv->cfg.max_edit_quads * 8 + 12ull * coord_cap + 4096;
+                            srv->cfg.max_edit_quads * 8 + 12ull * coord_cap + 4096 +
+                            (srv->cfg.keep_meshes ? 16ull * coord_cap : 0);
   const uint64_t budget = srv->cfg.hbm_budget_bytes ? srv->cfg.hbm_budget_bytes : ctx->budget_bytes;
-  const uint64_t scene_bytes = ctx->scene_bytes.load();
+  const uint64_t scene_bytes = ctx->scene_bytes.load() + store_bytes;
   if (budget <= scene_bytes || per_slot > budget - scene_bytes) {
+    for (meso_mesh_store* t : srv->stores) meso_mesh_store_destroy(ctx, t);
     delete srv;
     return fail(MESO_ERR_OVER_BUDGET, "server_create: HBM budget leaves no room for one batch slot");
   }
@@ -468,8 +530,15 @@ meso_status meso_server_create(meso_ctx* ctx, const meso_server_config* cfg, mes
     if (e == cudaSuccess) e = cudaMalloc(&s.d_coords, 12ull * std::max<uint32_t>(coord_cap, 1));
     if (e == cudaSuccess) e = cudaMallocHost(&s.h_coords, 12ull * std::max<uint32_t>(coord_cap, 1));
     if (e == cudaSuccess && srv->cfg.keep_hits) e = cudaMallocHost(&s.h_hits, srv->cfg.max_batch_rays * sizeof(meso_hit));
+    if (e == cudaSuccess && srv->cfg.keep_meshes) {
+      e = cudaMalloc(&s.d_counts, 4ull * std::max<uint32_t>(coord_cap, 1));
+      if (e == cudaSuccess) e = cudaMalloc(&s.d_place, 12ull * std::max<uint32_t>(coord_cap, 1));
+      if (e == cudaSuccess) e = cudaMallocHost(&s.h_flags, sizeof(unsigned long long));
+      if (e == cudaSuccess) *s.h_flags = 0;
+    }
     if (e != cudaSuccess) {
       for (auto& t : srv->slots) release_slot(t);
+      for (meso_mesh_store* t : srv->stores) meso_mesh_store_destroy(ctx, t);
       delete srv;
       return cuda_fail(e, "server_create: slot allocation");
     }
@@ -549,7 +618,16 @@ meso_status meso_server_destroy(meso_server* srv) {
   }
   if (srv->th.joinable()) srv->th.join();
   for (auto& s : srv->slots) release_slot(s);
+  for (meso_mesh_store* t : srv->stores) meso_mesh_store_destroy(srv->ctx, t);
   delete srv;
+  return MESO_OK;
+}
+
+meso_status meso_server_get_store(meso_server* srv, uint32_t scene_index, meso_mesh_store** out) {
+  if (!srv || !out) return fail(MESO_ERR_INVALID_ARG, "server_get_store: null argument");
+  if (srv->stores.empty()) return fail(MESO_ERR_INVALID_ARG, "server_get_store: the server keeps no meshes");
+  if (scene_index >= srv->stores.size()) return fail(MESO_ERR_INVALID_ARG, "server_get_store: bad scene index");
+  *out = srv->stores[scene_index];
   return MESO_OK;
 }
 

@@ -107,3 +107,91 @@ def test_admission_rejects_oversize_and_overflowing_queue(ctx):
     for i in ids:
         c = comp[i]
         assert c.done_s >= c.submit_s
+
+
+def _oracle_terrain(t):
+    import oracle
+    return oracle.terrain(t.nx, t.ny, t.nz, t.seed, t.height_period, t.height_octaves, t.height_base,
+                          t.height_amp, t.cave_period, t.cave_threshold)
+
+
+def test_served_edits_equal_oracle_replay(ctx):
+    """The served edit path -- sphere edits, the forked remesh and render,
+    the mesh store update, delivery into caller-owned buffers -- against a
+    sequential replay on the oracle: every delivered render equals the
+    oracle's raymarch of the scene as of that request (bit for bit), every
+    remesh's dirty count and quad hash equal the oracle's, and the server's
+    mesh store ends equal to the oracle's mesh of the final scene."""
+    import oracle
+    t = meso.terrain_preset("small")
+    scene = ctx.scene_from_terrain(t, spare_bricks=8192)
+    bm = oracle.HostBrickMap.from_terrain(_oracle_terrain(t))
+    reqs = [r for r in _requests(31, n=40) if r[0] == 0]
+    assert sum(1 for r in reqs if r[3]) >= 3
+    srv = meso.Server(ctx, [scene], max_inflight_batches=3, max_batch_rays=1 << 20, max_edit_quads=1 << 20,
+                      keep_meshes=1)
+    outs, ids = [], []
+    for i, (_, cam, shadow, ed) in enumerate(reqs):
+        outs.append(ctx.alloc(cam.width * cam.height * 24))
+        ids.append(srv.submit(0, cam, shadow=shadow, edits=ed, tag=i, dst=outs[-1]))
+    srv.drain()
+    comp = {c.user_tag: c for c in srv.poll()}
+    cx = t.nx // 32
+    for i, (_, cam, shadow, ed) in enumerate(reqs):
+        c = comp[i]
+        assert c.status == 0
+        if ed:
+            sp = [oracle.Sphere((ctypes.c_int32 * 3)(*e.center), e.radius, e.material, 0) for e in ed]
+            dirty = bm.dirty_chunks(sp)
+            bm.edit(sp)
+            assert c.n_dirty_chunks == len(dirty)
+            coords = np.stack([dirty % cx, (dirty // cx) % cx, dirty // (cx * cx)], 1).astype(np.int32)
+            q = oracle.mesh_chunks(oracle.SRC_BRICKMAP, coords=coords, bm=bm)
+            assert c.n_quads == len(q) and c.quad_checksum == meso.quad_checksum(q)
+        ref = oracle.raymarch(bm, _oracle_cam(cam), shadow=shadow)
+        got = outs[i].download(meso.HIT_DTYPE, cam.width * cam.height)
+        assert np.array_equal(got.view(np.uint8), ref.view(np.uint8)), f"request {i}"
+    n = (t.nx // 32) * (t.ny // 32) * (t.nz // 32)
+    idx = np.arange(n)
+    coords = np.stack([idx % cx, (idx // cx) % cx, idx // (cx * cx)], 1).astype(np.int32)
+    got = np.sort(srv.store(0).gather(idx))
+    assert np.array_equal(got, oracle.mesh_chunks(oracle.SRC_BRICKMAP, coords=coords, bm=bm))
+    srv.close()
+
+
+def _oracle_cam(cam):
+    """The oracle's camera with the same fields as a meso camera."""
+    import oracle
+    return oracle.Camera.from_buffer_copy(bytes(cam))  # the two structs share one layout
+
+
+def test_served_store_repaired_after_overflow(ctx):
+    """An edit whose remesh overflows the server's quad buffer (max_edit_quads
+    far too small) reports MESO_ERR_OVERFLOW for its quad count, and its
+    placement into the mesh store fails on the device; the server places
+    those chunks again before the scene's next request, so the store still
+    equals the oracle's mesh of the edited scene."""
+    import oracle
+    t = meso.terrain_preset("small")
+    scene = ctx.scene_from_terrain(t, spare_bricks=8192)
+    bm = oracle.HostBrickMap.from_terrain(_oracle_terrain(t))
+    srv = meso.Server(ctx, [scene], max_inflight_batches=2, max_batch_rays=1 << 16, max_edit_quads=256,
+                      keep_meshes=1)
+    cam = meso.camera((-40.0, -30.0, 140.0), (64.0, 64.0, 20.0), 32, 24)
+    eds = []
+    for k in range(3):
+        ed = [meso.SphereEdit((ctypes.c_int32 * 3)(20 + 40 * k, 60, 30), 14, 0 if k == 1 else 700 + k, 0),
+              meso.SphereEdit((ctypes.c_int32 * 3)(90, 20 + 30 * k, 25), 9, 1234 + k, 0)]
+        eds.append(ed)
+        srv.submit(0, cam, edits=ed, tag=k)
+    srv.drain()
+    comp = {c.user_tag: c for c in srv.poll()}
+    assert any(c.status == 4 for c in comp.values())  # MESO_ERR_OVERFLOW: the remesh did not fit 256 quads
+    for ed in eds:
+        bm.edit([oracle.Sphere((ctypes.c_int32 * 3)(*e.center), e.radius, e.material, 0) for e in ed])
+    cx = t.nx // 32
+    idx = np.arange((t.nx // 32) * (t.ny // 32) * (t.nz // 32))
+    coords = np.stack([idx % cx, (idx // cx) % cx, idx // (cx * cx)], 1).astype(np.int32)
+    assert np.array_equal(np.sort(srv.store(0).gather(idx)),
+                          oracle.mesh_chunks(oracle.SRC_BRICKMAP, coords=coords, bm=bm))
+    srv.close()
