@@ -963,7 +963,8 @@ def run_reference(args, world, rank, local, dist):
 def run_profile_case(case: str):
     """One kernel of interest after a few warm-up launches, for ncu captures:
     'ray' = the 1080p frame of the 1024^3 scene (3 warm-up launches + 1),
-    'mesh' = the 4096-chunk batched mesh (3 warm-up launches + 1)."""
+    'mesh' = the 4096-chunk batched mesh (3 warm-up launches + 1),
+    'meshbrick' = all 32768 chunks of the 1024^3 brick map (3 warm-up launches + 1)."""
     import mesoengine_gb300 as meso
     ctx = meso.Context(0)
     if case == "ray":
@@ -972,6 +973,12 @@ def run_profile_case(case: str):
         out = ctx.alloc(FRAME_W * FRAME_H * 24)
         for _ in range(4):
             ctx.raymarch(scene, cam, out=out, download=False)
+    elif case == "meshbrick":
+        scene = ctx.scene_from_terrain(meso.terrain_preset("scene1024"))
+        idx = np.arange(32 ** 3)
+        coords = np.stack([idx % 32, (idx // 32) % 32, idx // 1024], 1).astype(np.int32)
+        for _ in range(4):
+            ctx.mesh(meso.SRC_BRICKMAP, coords=coords, scene=scene, capacity=96 << 20)
     else:
         data, _ = ctx.generate_chunks_u16(MESH_CHUNKS, seed0=1)
         for _ in range(4):
@@ -983,7 +990,7 @@ def run_profile_case(case: str):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--profile", choices=["ray", "mesh"], default=None,
+    ap.add_argument("--profile", choices=["ray", "mesh", "meshbrick"], default=None,
                     help="run one small single-kernel case for an ncu capture and exit")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
