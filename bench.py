@@ -711,6 +711,30 @@ def bench_serve_render(ctx, meso, seconds, rate=2000.0):
     d = summarize(comps)
     d["workload"] = f"the first {seconds / 2:.0f} s of the same arrivals, hits delivered into page-locked host memory"
     d["delivered_gb_s"] = round(sum(c.n_rays for c in comps if c.status == 0) * 24 / d["span_s"] / 1e9, 1)
+    # the link's own rate for such copies: one 4K frame of hits (199 MB)
+    # copied device -> page-locked host memory, and four such copies at once
+    # on the server's four slot streams
+    big = dst[(3840, 2160)]
+    src_hits = ctx.alloc(big.nbytes)
+    L = meso._lib
+    streams = [ctx.stream() for _ in range(4)]
+    for k in range(2):
+        meso._check(L.meso_memcpy_d2h(ctx.handle, big.ptr, src_hits.ptr, big.nbytes, None))
+    ctx.sync()
+    t0 = time.perf_counter()
+    for k in range(5):
+        meso._check(L.meso_memcpy_d2h(ctx.handle, big.ptr, src_hits.ptr, big.nbytes, None))
+    ctx.sync()
+    one = big.nbytes * 5 / (time.perf_counter() - t0) / 1e9
+    t0 = time.perf_counter()
+    for k in range(5):
+        for st in streams:
+            meso._check(L.meso_memcpy_d2h(ctx.handle, big.ptr, src_hits.ptr, big.nbytes, st))
+    for st in streams:
+        ctx.sync(st)
+    four = big.nbytes * 20 / (time.perf_counter() - t0) / 1e9
+    d["link_d2h_gb_s"] = {"one_stream": round(one, 1), "four_streams": round(four, 1)}
+    src_hits.free()
     res["delivered"] = d
     for b_ in dst.values():
         b_.free()

@@ -338,10 +338,19 @@ __device__ __forceinline__ void prefetch_chunk(const MeshParams& p, const CUtens
   }
 }
 
+// The one-voxel occupancy halo around the chunk: 6 faces x 32 rows, a row
+// per ballot.  Each warp reads its 12 rows' voxels first (for a brick map a
+// pointer load and a dependent occupancy load each) so all of them are in
+// flight together, then ballots them.
 template <int KIND>
 __device__ __forceinline__ void compute_halos(MeshSmem& sm, const MeshParams& p, int warp, int lane) {
+  constexpr int kPer = 6 * 32 / kWarps;
+  static_assert(kPer * kWarps == 6 * 32, "halo rows split evenly over the warps");
   const int X = sm.coord[0] * 32, Y = sm.coord[1] * 32, Z = sm.coord[2] * 32;
-  for (int wi = warp; wi < 6 * 32; wi += kWarps) {
+  uint32_t solid[kPer];
+#pragma unroll
+  for (int i = 0; i < kPer; i++) {
+    const int wi = warp + kWarps * i;
     const int f = wi >> 5, k = wi & 31;
     int gx, gy, gz;
     switch (f) {
@@ -352,8 +361,13 @@ __device__ __forceinline__ void compute_halos(MeshSmem& sm, const MeshParams& p,
       case 4: gx = X + lane; gy = Y + k; gz = Z - 1; break;
       default: gx = X + lane; gy = Y + k; gz = Z + 32; break;
     }
-    const uint32_t w = __ballot_sync(kFull, global_solid<KIND>(p, gx, gy, gz) != 0);
-    if (lane == 0) sm.halo[f][k] = w;
+    solid[i] = global_solid<KIND>(p, gx, gy, gz);
+  }
+#pragma unroll
+  for (int i = 0; i < kPer; i++) {
+    const int wi = warp + kWarps * i;
+    const uint32_t w = __ballot_sync(kFull, solid[i] != 0);
+    if (lane == 0) sm.halo[wi >> 5][wi & 31] = w;
   }
 }
 

@@ -189,6 +189,33 @@ def test_brickmap_chunks(ctx):
     assert np.array_equal(_sorted(q), ref)
 
 
+def test_brickmap_counts_with_empty_repeated_and_bad_chunks(ctx):
+    """Brick-map chunks are taken from the queue 32 at a time and tested
+    against the scene's per-chunk occupancy: empty chunks get count 0 without
+    being meshed, repeated chunks are meshed again, and an out-of-range
+    coordinate gets count 0 and raises the invalid-argument flag."""
+    t = meso.terrain_preset("small")
+    scene = ctx.scene_from_terrain(t)
+    bm = oracle.HostBrickMap.from_dense(scene.dense())
+    allc = [(x, y, z) for z in range(4) for y in range(4) for x in range(4)]
+    rng = np.random.default_rng(5)
+    good = [allc[i] for i in rng.integers(0, 64, 90)] + allc  # > 32, with repeats and empty chunks
+    coords = np.array(good + [(9, 0, 0)] + good[:7], dtype=np.int32)
+    with pytest.raises(meso.MesoError, match="outside"):
+        ctx.mesh(meso.SRC_BRICKMAP, coords=coords, scene=scene)
+    q, counts = ctx.mesh(meso.SRC_BRICKMAP, coords=coords, scene=scene, chunk_counts=True, check=False)
+    ok = np.array([i for i in range(len(coords)) if i != len(good)])
+    ref = oracle.mesh_chunks(oracle.SRC_BRICKMAP, coords=coords[ok], bm=bm)
+    ref_counts = np.bincount((ref >> np.uint64(44)).astype(np.int64), minlength=len(ok))
+    assert counts[len(good)] == 0
+    assert np.array_equal(counts[ok], ref_counts)
+    # quads carry the index in the call: map the oracle's indices back
+    chunk = (ref >> np.uint64(44)).astype(np.int64)
+    remapped = (ref & np.uint64((1 << 44) - 1)) | (ok[chunk].astype(np.uint64) << np.uint64(44))
+    assert np.array_equal(_sorted(q), np.sort(remapped))
+    assert (counts == 0).sum() > 1  # empty chunks among them
+
+
 def test_matches_golden_fixture(ctx):
     import os
     golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
