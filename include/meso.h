@@ -225,7 +225,11 @@ meso_status meso_mesh_chunks(meso_ctx* ctx, const meso_mesh_source* src, const i
 meso_status meso_mesh_chunks_per_launch(meso_ctx* ctx, const meso_mesh_source* src,
                                         const int32_t* d_chunk_coords, uint32_t n_chunks,
                                         const meso_mesh_output* out, void* stream);
-/* Synchronises stream, reads the quad count and the device error flag. */
+/* Synchronises stream, reads the quad count (always written to *h_count)
+ * and the device error flag: MESO_ERR_INVALID_ARG when a chunk coordinate or
+ * index was outside the source (that chunk yields no quads and count 0; the
+ * other chunks' quads are in the buffer), MESO_ERR_OVERFLOW when the count
+ * exceeds the capacity. */
 meso_status meso_mesh_check(meso_ctx* ctx, const meso_mesh_output* out, void* stream, uint64_t* h_count);
 /* Host-buffer form for callers that hold no device memory: copies the
  * chunk array (kind CHUNKS_U16/U8; nx chunks, or n_chunks when nx is 0) or
@@ -343,7 +347,8 @@ typedef struct meso_mesh_store_info {
 /* Meshes every non-empty chunk of the scene into a new store (waits). */
 meso_status meso_mesh_store_create(meso_ctx* ctx, const meso_scene* scene, meso_mesh_store** out);
 /* Remeshes the n listed chunks (linear indices, e.g. the dirty list of
- * meso_edit_spheres) in one batched launch and replaces their segments: in
+ * meso_edit_spheres; repeats are meshed once) in one batched launch and
+ * replaces their segments: in
  * place when the new quads fit, else at the arena's end; a full arena is
  * repacked (and grown) before the update completes.  Returns when the store
  * holds the new segments. */

@@ -417,8 +417,11 @@ meso_status meso_mesh_check(meso_ctx* ctx, const meso_mesh_output* out, void* st
   cudaStream_t st = pick_stream(ctx, stream);
   uint64_t cnt = 0;
   MESO_CUDA_TRY(cudaMemcpyAsync(&cnt, out->d_quad_count, 8, cudaMemcpyDeviceToHost, st));
-  MESO_TRY(meso_sync(ctx, st));
+  MESO_CUDA_TRY(cudaStreamSynchronize(st));
+  // the count is reported even when a device flag (e.g. a bad chunk
+  // coordinate, whose chunk produced nothing) makes the call fail
   if (h_count) *h_count = cnt;
+  MESO_TRY(meso_sync(ctx, st));
   if (cnt > out->capacity) return fail(MESO_ERR_OVERFLOW, "mesh: quad buffer too small");
   return MESO_OK;
 }

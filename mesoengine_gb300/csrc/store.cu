@@ -260,7 +260,10 @@ static meso_status compact(meso_ctx* ctx, meso_mesh_store* S, uint64_t min_cap, 
 // buffer requires.
 meso_status store_update_sync(meso_ctx* ctx, meso_mesh_store* S, const uint32_t* h_chunks, uint32_t n,
                               cudaStream_t st) {
+  // a chunk listed twice would be placed twice at once: keep one of each
   std::vector<uint32_t> todo(h_chunks, h_chunks + n);
+  std::sort(todo.begin(), todo.end());
+  todo.erase(std::unique(todo.begin(), todo.end()), todo.end());
   uint64_t temp_cap = 0;
   for (int round = 0; round < 8 && !todo.empty(); round++) {
     for (uint32_t c : todo)

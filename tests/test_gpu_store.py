@@ -78,8 +78,10 @@ def test_store_repacks_when_full(ctx):
         store.update(dirty)
     assert store.info().compactions >= 1
     _assert_store_matches(store, bm, dims)
-    # an update of no chunks and of unchanged chunks keeps everything
+    # an update of no chunks, of unchanged chunks and of a list with repeats
+    # keeps everything
     store.update([])
     store.update(np.arange(8))
+    store.update(np.array([3, 9, 3, 3, 40, 9], np.uint32))
     _assert_store_matches(store, bm, dims)
     store.destroy()
