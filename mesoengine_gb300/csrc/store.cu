@@ -209,8 +209,11 @@ static meso_status compact(meso_ctx* ctx, meso_mesh_store* S, uint64_t min_cap, 
   uint64_t top = 0;
   unplaced.clear();
   for (uint64_t c = 0; c < N; c++) {
-    if (cnt[c] == 0 && off[c] == kInvalidOff) continue;
-    if (off[c] == kInvalidOff) unplaced.push_back((uint32_t)c);
+    if (off[c] == kInvalidOff) {
+      // a chunk whose placement failed gets its segment when it is placed again
+      if (cnt[c]) unplaced.push_back((uint32_t)c);
+      continue;
+    }
     ncap[c] = slack_cap(cnt[c]);
     noff[c] = top;
     top += ncap[c];
@@ -226,8 +229,6 @@ static meso_status compact(meso_ctx* ctx, meso_mesh_store* S, uint64_t min_cap, 
     ctx->launches.fetch_add(1);
     e = cudaGetLastError();
   }
-  // placed chunks keep their segments; unplaced ones get theirs when remeshed
-  for (uint32_t c : unplaced) noff[c] = kInvalidOff, ncap[c] = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(S->d_off, noff.data(), N * 8, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(S->d_cap, ncap.data(), N * 4, cudaMemcpyHostToDevice, st);
   unsigned long long state[3] = {top, 0, 0};
