@@ -195,3 +195,30 @@ def test_served_store_repaired_after_overflow(ctx):
     assert np.array_equal(np.sort(srv.store(0).gather(idx)),
                           oracle.mesh_chunks(oracle.SRC_BRICKMAP, coords=coords, bm=bm))
     srv.close()
+
+
+def test_served_stores_of_two_scenes(ctx):
+    """keep_meshes with two resident scenes: edits of either scene, mixed in
+    one stream, leave each scene's store equal to the oracle's mesh of that
+    scene after its own edits."""
+    import oracle
+    scenes = _scenes(ctx)
+    presets = [meso.terrain_preset("small"), meso.Terrain(256, 256, 128, 21, 128, 6, 10.0, 48.0, 48, 0.7)]
+    bms = [oracle.HostBrickMap.from_terrain(_oracle_terrain(t)) for t in presets]
+    reqs = _requests(44, n=30)
+    srv = meso.Server(ctx, scenes, max_inflight_batches=3, max_batch_rays=1 << 20, max_edit_quads=1 << 20,
+                      keep_meshes=1)
+    for i, (sc, cam, shadow, ed) in enumerate(reqs):
+        srv.submit(sc, cam, shadow=shadow, edits=ed, tag=i)
+        if ed:
+            bms[sc].edit([oracle.Sphere((ctypes.c_int32 * 3)(*e.center), e.radius, e.material, 0) for e in ed])
+    srv.drain()
+    assert all(c.status == 0 for c in srv.poll())
+    assert sum(1 for r in reqs if r[3] and r[0] == 0) > 0 and sum(1 for r in reqs if r[3] and r[0] == 1) > 0
+    for k, t in enumerate(presets):
+        cx, cy, cz = t.nx // 32, t.ny // 32, t.nz // 32
+        idx = np.arange(cx * cy * cz)
+        coords = np.stack([idx % cx, (idx // cx) % cy, idx // (cx * cy)], 1).astype(np.int32)
+        assert np.array_equal(np.sort(srv.store(k).gather(idx)),
+                              oracle.mesh_chunks(oracle.SRC_BRICKMAP, coords=coords, bm=bms[k]))
+    srv.close()

@@ -85,3 +85,27 @@ def test_store_repacks_when_full(ctx):
     store.update(np.array([3, 9, 3, 3, 40, 9], np.uint32))
     _assert_store_matches(store, bm, dims)
     store.destroy()
+
+
+def test_store_of_empty_scene_and_emptied_scene(ctx):
+    """A scene with no solid voxel has an empty store; a scene whose every
+    solid voxel is removed by edits ends with an empty store; refilling it
+    brings the quads back, each time equal to the oracle."""
+    g = np.zeros((64, 64, 64), np.uint16)
+    scene = ctx.scene_from_dense(g, spare_bricks=4096)
+    bm = oracle.HostBrickMap.from_dense(g)
+    store = ctx.mesh_store(scene)
+    assert store.info().live_quads == 0
+    assert store.gather(np.arange(8)).size == 0
+    fill = [((32, 32, 32), 20, 77), ((10, 50, 20), 6, 5)]
+    dirty = scene.edit([meso.SphereEdit((ctypes.c_int32 * 3)(*c), r, m, 0) for c, r, m in fill])
+    bm.edit([oracle.Sphere((ctypes.c_int32 * 3)(*c), r, m, 0) for c, r, m in fill])
+    store.update(dirty)
+    _assert_store_matches(store, bm, (64, 64, 64))
+    clear = [((32, 32, 32), 60, 0)]
+    dirty = scene.edit([meso.SphereEdit((ctypes.c_int32 * 3)(*c), r, m, 0) for c, r, m in clear])
+    bm.edit([oracle.Sphere((ctypes.c_int32 * 3)(*c), r, m, 0) for c, r, m in clear])
+    store.update(dirty)
+    assert store.info().live_quads == 0
+    _assert_store_matches(store, bm, (64, 64, 64))
+    store.destroy()
