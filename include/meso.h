@@ -397,8 +397,13 @@ typedef struct meso_request {
   const meso_sphere_edit* edits; /* copied at submit */
   uint64_t user_tag;
   meso_hit* dst_hits;       /* optional caller-owned destination of the request's
-                               width*height hits: device memory or page-locked host
-                               memory; the completion is reported after they land */
+                               width*height hits, reported complete after they land.
+                               Device memory of the server's device or page-locked
+                               host memory, 8-byte aligned: the raymarch kernel
+                               stores into it directly.  Anything else (pageable
+                               memory, unaligned, or a keep_hits server): one copy
+                               from the batch buffer.  Resolved at submit; the
+                               buffer must stay valid until the completion. */
 } meso_request;
 
 typedef struct meso_completion {

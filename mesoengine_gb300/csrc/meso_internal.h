@@ -124,10 +124,18 @@ meso_status rebuild_macro(meso_ctx* ctx, meso_scene* s, const uint32_t* d_cells,
 meso_status launch_mesh(meso_ctx* ctx, const meso_mesh_source* src, const int32_t* d_coords,
                         uint32_t n_chunks, const meso_mesh_output* out, cudaStream_t st, bool per_launch);
 struct RayView;
+// view_out (optional, n_views entries): where view v's hits go, a device or
+// device-mapped address aligned to 8 bytes; a null entry (or a null array)
+// keeps the view's place in d_hits (views packed in order).  d_hash
+// (optional; at most kRayHashViews views, not with d_stats): the kernel adds
+// view v's order-sensitive hit checksum into d_hash[v] and its traced shadow
+// rays into d_hash[kRayHashViews + v].
+constexpr uint32_t kRayHashViews = 64;
 meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* cams,
                             uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
                             cudaStream_t st, void* d_view_table, size_t view_table_bytes,
-                            uint64_t* d_stats = nullptr);
+                            uint64_t* d_stats = nullptr, meso_hit* const* view_out = nullptr,
+                            unsigned long long* d_hash = nullptr);
 size_t raymarch_view_table_bytes(uint32_t n_views);
 
 // Mesh store internals shared with the serving loop (store.cu).

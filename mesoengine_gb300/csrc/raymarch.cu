@@ -36,7 +36,7 @@ struct RayView {
   uint32_t width, height;
   uint32_t tiles_x;
   uint32_t tile_start;
-  uint64_t hit_offset;
+  meso_hit* out;  // this view's width*height hit records, row major
 };
 
 namespace {
@@ -44,7 +44,19 @@ namespace {
 using namespace ::meso::dev;
 
 constexpr int kInlineViews = 32;
+constexpr int kPlain = 0, kStatsMode = 1, kHashMode = 2;
+constexpr uint32_t kFullMask = 0xFFFFFFFFu;
 constexpr float kInf = __builtin_huge_valf();
+
+// splitmix64 finaliser (the hit checksum's mixing function)
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  x ^= x >> 30;
+  x *= 0xBF58476D1CE4E5B9ull;
+  x ^= x >> 27;
+  x *= 0x94D049BB133111EBull;
+  x ^= x >> 31;
+  return x;
+}
 
 struct InlineViews {
   RayView v[kInlineViews];
@@ -58,8 +70,8 @@ struct RayParams {
   float light[3];
   float inv_light[3];  // 1 / light per axis, correctly rounded (0 for a zero component)
   uint32_t shadow;
-  meso_hit* hits;
   uint64_t* stats;
+  unsigned long long* hash;  // checksum instantiation: [v] hit hash, [kRayHashViews + v] traced shadow rays
   uint32_t order_mul;  // CTA b takes block (b * order_mul) mod gridDim.x (0: block b)
 };
 
@@ -478,12 +490,16 @@ __device__ __forceinline__ void trace_pixel(const RayView& V, uint32_t px, uint3
 }
 
 
-// kStats: also accumulates {pointer fetches, occupied bricks entered, hits,
-// rays} into P.stats (a separate instantiation; the timed path has none of it).
+// kMode: kPlain; kStatsMode also accumulates {pointer fetches, occupied
+// bricks entered, hits, rays} into P.stats; kHashMode also adds each view's
+// order-sensitive hit checksum and its traced shadow rays into P.hash (the
+// serving loop's per-request summary, so the hits need not be read again).
+// Each is a separate instantiation; the timed path has none of it.
 // At most 128 threads per CTA; 8 resident CTAs per SM cap registers at 64,
 // which measured faster than the uncapped 73 (more warps to hide latency).
-template <bool kInline, bool kStats>
+template <bool kInline, int kMode>
 __global__ void __launch_bounds__(128, 8) raymarch_kernel(const RayParams P, const __grid_constant__ InlineViews iv) {
+  constexpr bool kStats = kMode == kStatsMode;
   const uint32_t warps = blockDim.x >> 5;
   const uint32_t bid = P.order_mul ? (uint32_t)(((uint64_t)blockIdx.x * P.order_mul) % gridDim.x) : blockIdx.x;
   const uint32_t tile = bid * warps + (threadIdx.x >> 5);
@@ -520,7 +536,7 @@ __global__ void __launch_bounds__(128, 8) raymarch_kernel(const RayParams P, con
   }
   __syncwarp();
   const uint32_t row_words = 3 * P.tile_w;
-  uint64_t* base = reinterpret_cast<uint64_t*>(P.hits + V.hit_offset);
+  uint64_t* base = reinterpret_cast<uint64_t*>(V.out);
   // a whole tile whose rows all start on 16 bytes goes out in 16-byte stores
   const bool vec = ((reinterpret_cast<uintptr_t>(base) + (((uint64_t)py0 * V.width + px0) * 24)) & 15u) == 0 &&
                    (V.width & 1u) == 0 && (P.tile_w & 1u) == 0 && px0 + P.tile_w <= V.width &&
@@ -551,6 +567,23 @@ __global__ void __launch_bounds__(128, 8) raymarch_kernel(const RayParams P, con
       if (lane == 0) atomicAdd(reinterpret_cast<unsigned long long*>(P.stats) + k, (unsigned long long)tot);
     }
   }
+  if constexpr (kMode == kHashMode) {
+    unsigned long long term = 0;
+    uint32_t shadow = 0;
+    if (px < V.width && py < V.height) {
+      const uint64_t i = (uint64_t)py * V.width + px;
+      const uint64_t w0 = sw[3 * lane], w1 = sw[3 * lane + 1], w2 = sw[3 * lane + 2];
+      term = mix64(w0 ^ mix64(w1 ^ mix64(w2 ^ (i * 0x9E3779B97F4A7C15ull + 1ull))));
+      shadow = (w2 >> 32) != 0;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) term += __shfl_down_sync(kFullMask, term, o);
+    shadow = __reduce_add_sync(kFullMask, shadow);
+    if (lane == 0) {
+      atomicAdd(P.hash + lo, term);
+      atomicAdd(P.hash + kRayHashViews + lo, (unsigned long long)shadow);
+    }
+  }
 }
 
 }  // namespace
@@ -569,7 +602,7 @@ static uint32_t block_order_mul(uint32_t blocks) { return blocks > 1 && blocks %
 // and hits are running totals over all views of the launch (in: those of
 // the views before these; out: including them).
 static void fill_views(const meso_scene* const* scenes, const meso_camera* cams, uint32_t n, uint32_t tw, uint32_t th,
-                       RayView* out, uint64_t& tiles, uint64_t& hits) {
+                       meso_hit* d_hits, meso_hit* const* view_out, RayView* out, uint64_t& tiles, uint64_t& hits) {
   for (uint32_t v = 0; v < n; v++) {
     const meso_scene* s = scenes[v];
     const meso_camera& c = cams[v];
@@ -598,7 +631,7 @@ static void fill_views(const meso_scene* const* scenes, const meso_camera* cams,
     V.tiles_x = (c.width + tw - 1) / tw;
     const uint32_t tiles_y = (c.height + th - 1) / th;
     V.tile_start = (uint32_t)tiles;
-    V.hit_offset = hits;
+    V.out = view_out && view_out[v] ? view_out[v] : d_hits + hits;
     tiles += (uint64_t)V.tiles_x * tiles_y;
     hits += (uint64_t)c.width * c.height;
   }
@@ -634,12 +667,13 @@ __global__ void view_fill_kernel(const __grid_constant__ ViewBatch b, uint32_t n
 // views, the descriptors travelling as its parameters.  *tiles receives the
 // total tiles of the views.
 static meso_status stage_view_table(const meso_scene* const* scenes, const meso_camera* cams, uint32_t n_views,
-                                    uint32_t tw, uint32_t th, RayView* d_table, cudaStream_t st, uint64_t* tiles) {
+                                    uint32_t tw, uint32_t th, meso_hit* d_hits, meso_hit* const* view_out,
+                                    RayView* d_table, cudaStream_t st, uint64_t* tiles) {
   ViewBatch batch;
   uint64_t t = 0, hits = 0;
   for (uint32_t v0 = 0; v0 < n_views; v0 += kFillViews) {
     const uint32_t n = n_views - v0 < kFillViews ? n_views - v0 : kFillViews;
-    fill_views(scenes + v0, cams + v0, n, tw, th, batch.v, t, hits);
+    fill_views(scenes + v0, cams + v0, n, tw, th, d_hits, view_out ? view_out + v0 : nullptr, batch.v, t, hits);
     view_fill_kernel<<<1, 128, 0, st>>>(batch, n, d_table + v0);
     MESO_CUDA_TRY(cudaGetLastError());
   }
@@ -649,14 +683,19 @@ static meso_status stage_view_table(const meso_scene* const* scenes, const meso_
 
 meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* cams,
                             uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
-                            cudaStream_t st, void* d_view_table, size_t view_table_bytes, uint64_t* d_stats) {
+                            cudaStream_t st, void* d_view_table, size_t view_table_bytes, uint64_t* d_stats,
+                            meso_hit* const* view_out, unsigned long long* d_hash) {
   if (!scenes || !cams || !d_hits) return fail(MESO_ERR_INVALID_ARG, "raymarch: null argument");
   if (n_views == 0) return MESO_OK;
   for (uint32_t v = 0; v < n_views; v++) {
     if (!scenes[v]) return fail(MESO_ERR_INVALID_ARG, "raymarch: null scene");
     if (cams[v].width == 0 || cams[v].height == 0 || cams[v].width > 16384 || cams[v].height > 16384)
       return fail(MESO_ERR_INVALID_ARG, "raymarch: image size out of range");
+    if (view_out && (reinterpret_cast<uintptr_t>(view_out[v]) & 7u))
+      return fail(MESO_ERR_INVALID_ARG, "raymarch: view output not 8-byte aligned");
   }
+  if (d_hash && (d_stats || n_views > kRayHashViews))
+    return fail(MESO_ERR_INVALID_ARG, "raymarch: checksums need at most 64 views and no statistics");
   if ((flags & MESO_RAY_SHADOW) && !light) return fail(MESO_ERR_INVALID_ARG, "raymarch: shadow without light");
   const uint32_t tw = ctx->tuning.ray_tile_w ? ctx->tuning.ray_tile_w : 8;
   if (32 % tw) return fail(MESO_ERR_INVALID_ARG, "raymarch: tile width must divide 32");
@@ -673,32 +712,35 @@ meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, cons
       P.light[a] = light[a];
       P.inv_light[a] = light[a] != 0.0f ? 1.0f / light[a] : 0.0f;  // IEEE division, as __fdiv_rn
     }
-  P.hits = d_hits;
   P.stats = d_stats;
+  P.hash = d_hash;
   static InlineViews empty_views;  // zero-initialised
   uint64_t tiles;
   if (n_views <= (uint32_t)kInlineViews) {
     InlineViews iv;
     tiles = 0;
     uint64_t hits = 0;
-    fill_views(scenes, cams, n_views, tw, th, iv.v, tiles, hits);
+    fill_views(scenes, cams, n_views, tw, th, d_hits, view_out, iv.v, tiles, hits);
     if (tiles >= (1ull << 31)) return fail(MESO_ERR_INVALID_ARG, "raymarch: too many tiles");
     P.total_tiles = (uint32_t)tiles;
     const uint32_t blocks = (uint32_t)((tiles + wpc - 1) / wpc);
     P.order_mul = block_order_mul(blocks);
-    if (d_stats) raymarch_kernel<true, true><<<blocks, wpc * 32, 0, st>>>(P, iv);
-    else raymarch_kernel<true, false><<<blocks, wpc * 32, 0, st>>>(P, iv);
+    if (d_stats) raymarch_kernel<true, kStatsMode><<<blocks, wpc * 32, 0, st>>>(P, iv);
+    else if (d_hash) raymarch_kernel<true, kHashMode><<<blocks, wpc * 32, 0, st>>>(P, iv);
+    else raymarch_kernel<true, kPlain><<<blocks, wpc * 32, 0, st>>>(P, iv);
   } else {
     if (!d_view_table || view_table_bytes < raymarch_view_table_bytes(n_views))
       return fail(MESO_ERR_INVALID_ARG, "raymarch: view table too small");
-    MESO_TRY(stage_view_table(scenes, cams, n_views, tw, th, static_cast<RayView*>(d_view_table), st, &tiles));
+    MESO_TRY(stage_view_table(scenes, cams, n_views, tw, th, d_hits, view_out, static_cast<RayView*>(d_view_table),
+                              st, &tiles));
     if (tiles >= (1ull << 31)) return fail(MESO_ERR_INVALID_ARG, "raymarch: too many tiles");
     P.total_tiles = (uint32_t)tiles;
     P.table = static_cast<const RayView*>(d_view_table);
     const uint32_t blocks = (uint32_t)((tiles + wpc - 1) / wpc);
     P.order_mul = block_order_mul(blocks);
-    if (d_stats) raymarch_kernel<false, true><<<blocks, wpc * 32, 0, st>>>(P, empty_views);
-    else raymarch_kernel<false, false><<<blocks, wpc * 32, 0, st>>>(P, empty_views);
+    if (d_stats) raymarch_kernel<false, kStatsMode><<<blocks, wpc * 32, 0, st>>>(P, empty_views);
+    else if (d_hash) raymarch_kernel<false, kHashMode><<<blocks, wpc * 32, 0, st>>>(P, empty_views);
+    else raymarch_kernel<false, kPlain><<<blocks, wpc * 32, 0, st>>>(P, empty_views);
   }
   ctx->launches.fetch_add(1);
   MESO_CUDA_TRY(cudaGetLastError());
@@ -801,13 +843,13 @@ extern "C" meso_status meso_raymarch_noalloc(meso_ctx* ctx, const meso_scene* co
       P.light[a] = light[a];
       P.inv_light[a] = light[a] != 0.0f ? 1.0f / light[a] : 0.0f;  // IEEE division, as __fdiv_rn
     }
-  P.hits = d_hits;
   const cudaStream_t st = pick_stream(ctx, stream);
-  MESO_TRY(stage_view_table(scenes, h_cams, n_views, tw, th, static_cast<RayView*>(table), st, &tiles));
+  MESO_TRY(stage_view_table(scenes, h_cams, n_views, tw, th, d_hits, nullptr, static_cast<RayView*>(table), st,
+                            &tiles));
   static InlineViews unused_inline;  // zero-initialised; the table path does not read it
   const uint32_t blocks = (uint32_t)((tiles + wpc - 1) / wpc);
   P.order_mul = block_order_mul(blocks);
-  raymarch_kernel<false, false><<<blocks, wpc * 32, 0, st>>>(P, unused_inline);
+  raymarch_kernel<false, kPlain><<<blocks, wpc * 32, 0, st>>>(P, unused_inline);
   ctx->launches.fetch_add(1);
   MESO_CUDA_TRY(cudaGetLastError());
   return MESO_OK;

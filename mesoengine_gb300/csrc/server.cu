@@ -20,8 +20,13 @@
 //    before an edit may run with other renders; one that arrived after waits
 //    for the edit), so every result equals a sequential replay;
 //  - results are summarised on the device (order-sensitive hash of the hit
-//    buffer, order-insensitive hash of the quads, traced shadow rays) and the
-//    hits can be kept for meso_server_fetch_hits;
+//    buffer and traced shadow rays, computed by the raymarch kernel itself;
+//    order-insensitive hash of the quads) and the hits can be kept for
+//    meso_server_fetch_hits;
+//  - a request's hits go straight to its dst_hits when that is device memory
+//    of the server's device or device-mapped page-locked host memory (the
+//    kernel's stores cross the CPU-GPU link while it traces); other
+//    destinations get a copy from the batch buffer;
 //  - a request that can never fit a slot, or that arrives when max_queue
 //    requests are already waiting, completes at once with
 //    MESO_ERR_OVER_BUDGET.
@@ -48,6 +53,7 @@ namespace meso {
 namespace {
 
 constexpr uint32_t kMaxBatch = 64;
+static_assert(kMaxBatch == kRayHashViews, "the raymarch kernel sums checksums of at most one batch of views");
 
 __device__ __forceinline__ uint64_t mix64(uint64_t x) {
   // splitmix64 finaliser
@@ -57,35 +63,6 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
   x *= 0x94D049BB133111EBull;
   x ^= x >> 31;
   return x;
-}
-
-struct HashSegs {
-  uint64_t off[kMaxBatch];
-  uint64_t cnt[kMaxBatch];
-  uint32_t n;
-};
-
-// out[s] += sum_i mix64(w0 ^ mix64(w1 ^ mix64(w2 ^ (i*K + 1)))) over hit i of
-// segment s (i relative to the segment); out[kMaxBatch + s] += traced shadow rays.
-__global__ void hit_hash_kernel(const uint64_t* words, const HashSegs S, unsigned long long* out) {
-  const uint32_t seg = blockIdx.y;
-  if (seg >= S.n) return;
-  const uint64_t base = S.off[seg], cnt = S.cnt[seg];
-  unsigned long long acc = 0, shadows = 0;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t* w = words + (base + i) * 3;
-    const uint64_t w0 = w[0], w1 = w[1], w2 = w[2];
-    acc += mix64(w0 ^ mix64(w1 ^ mix64(w2 ^ (i * 0x9E3779B97F4A7C15ull + 1ull))));
-    shadows += (w2 >> 32) != 0;
-  }
-  for (int o = 16; o; o >>= 1) {
-    acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
-    shadows += __shfl_down_sync(0xFFFFFFFFu, shadows, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(out + seg, acc);
-    atomicAdd(out + kMaxBatch + seg, shadows);
-  }
 }
 
 // out[0] += sum mix64(q) over the min(count, cap) quads.
@@ -105,6 +82,7 @@ struct SrvRequest {
   std::vector<meso_sphere_edit> edits;
   double submit = 0;
   uint64_t pixels = 0;
+  meso_hit* d_dst = nullptr;  // device address the kernel may store dst_hits through (null: copy)
 };
 
 struct Slot {
@@ -259,15 +237,14 @@ void launch_batch(meso_server* srv, Slot& s) {
   cudaMemsetAsync(s.d_sums, 0, sizeof(unsigned long long) * (2 * kMaxBatch + 2), st);
   std::vector<const meso_scene*> scenes;
   std::vector<meso_camera> cams;
-  HashSegs segs;
-  memset(&segs, 0, sizeof(segs));
+  std::vector<meso_hit*> view_out;
+  bool direct = false;
   uint64_t off = 0;
   for (auto& r : s.reqs) {
     scenes.push_back(srv->scenes[r.req.scene_index]);
     cams.push_back(r.req.camera);
-    segs.off[segs.n] = off;
-    segs.cnt[segs.n] = r.pixels;
-    segs.n++;
+    view_out.push_back(r.d_dst);
+    direct = direct || r.d_dst;
     s.offsets.push_back(off);
     off += r.pixels;
   }
@@ -303,8 +280,10 @@ void launch_batch(meso_server* srv, Slot& s) {
       meso_mesh_store* store = srv->stores.empty() ? nullptr : srv->stores[r.req.scene_index];
       o.d_chunk_quad_counts = store ? s.d_counts : nullptr;
       rc = launch_mesh(ctx, &src, s.d_coords, n_dirty, &o, st, false);
-      if (rc == MESO_OK)
+      if (rc == MESO_OK) {
         quad_hash_kernel<<<64, 256, 0, st>>>(s.d_quads, o.d_quad_count, s.quad_cap, s.d_sums + 2 * kMaxBatch);
+        ctx->launches.fetch_add(1);
+      }
       // the scene's resident mesh: the dirty chunks' new quads replace their
       // segments; a failed placement is flagged and repaired at completion
       if (rc == MESO_OK && store)
@@ -321,17 +300,15 @@ void launch_batch(meso_server* srv, Slot& s) {
   const cudaStream_t rs = s.edit ? s.stream2 : st;  // the render's stream
   if (rc == MESO_OK)
     rc = launch_raymarch(ctx, scenes.data(), cams.data(), (uint32_t)cams.size(), srv->light, s.reqs[0].req.flags,
-                         s.d_hits, rs, s.d_table, s.table_bytes);
+                         s.d_hits, rs, s.d_table, s.table_bytes, nullptr, direct ? view_out.data() : nullptr,
+                         s.d_sums);
   if (rc == MESO_OK) {
-    // about eight CTAs per SM over the batch, at least eight per request
-    const uint32_t per_seg = std::max<uint32_t>(8u, ((uint32_t)ctx->sm_count * 8u + segs.n - 1) / segs.n);
-    dim3 grid(std::min<uint32_t>(per_seg, 1024u), segs.n);
-    hit_hash_kernel<<<grid, 256, 0, rs>>>(reinterpret_cast<const uint64_t*>(s.d_hits), segs, s.d_sums);
-    ctx->launches.fetch_add(s.edit ? 2 : 1);
-    // delivery into the callers' buffers, before the completion is signalled
+    // delivery into the callers' buffers that the kernel could not store
+    // into, before the completion is signalled
     for (size_t k = 0; k < s.reqs.size(); k++) {
       meso_hit* dst = s.reqs[k].req.dst_hits;
-      if (dst) cudaMemcpyAsync(dst, s.d_hits + s.offsets[k], s.reqs[k].pixels * sizeof(meso_hit), cudaMemcpyDefault, rs);
+      if (dst && !s.reqs[k].d_dst)
+        cudaMemcpyAsync(dst, s.d_hits + s.offsets[k], s.reqs[k].pixels * sizeof(meso_hit), cudaMemcpyDefault, rs);
     }
     if (s.edit) {
       cudaEventRecord(s.joined, rs);
@@ -563,6 +540,21 @@ meso_status meso_server_submit(meso_server* srv, const meso_request* req, uint64
   r.req.edits = nullptr;
   if (req->kind == MESO_REQ_EDIT_REMESH_RENDER) r.edits.assign(req->edits, req->edits + req->n_edits);
   r.pixels = pixels_of(c);
+  // a destination the raymarch kernel can store into directly (kept hits
+  // are read from the batch buffer, so they keep every view there)
+  if (req->dst_hits && !srv->cfg.keep_hits) {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, req->dst_hits) == cudaSuccess) {
+      void* dp = nullptr;
+      if ((pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged) && pa.device == srv->ctx->device)
+        dp = pa.devicePointer;
+      else if (pa.type == cudaMemoryTypeHost)
+        dp = pa.devicePointer;
+      if (dp && !(reinterpret_cast<uintptr_t>(dp) & 7u)) r.d_dst = static_cast<meso_hit*>(dp);
+    } else {
+      cudaGetLastError();
+    }
+  }
   std::lock_guard<std::mutex> lk(srv->mu);
   r.id = srv->next_id++;
   r.submit = srv->now();

@@ -77,6 +77,50 @@ def test_render_results_equal_alone_and_in_mix(ctx):
         assert mix[i].n_rays == cam.width * cam.height + np.count_nonzero(direct["shadow_steps"])
 
 
+def test_delivery_to_every_destination_kind(ctx):
+    """Delivered hits and their checksums do not depend on where they go.
+    The raymarch kernel stores a request's hits straight into device memory
+    or device-mapped page-locked host memory (aligned to 8 bytes); any other
+    destination (pageable host memory, an address off the 8-byte grid) gets
+    a copy from the batch buffer.  Batches mix all kinds; every delivered
+    buffer equals a direct raymarch, bit for bit, and every completion's
+    checksum and ray count equal the host hash of those hits."""
+    reqs = _requests(5, n=30, edits=False)
+    scenes = _scenes(ctx)
+    srv = meso.Server(ctx, scenes, max_inflight_batches=2, max_batch_rays=1 << 20)
+    keep, dsts = [], []
+    for i, (sc, cam, shadow, _) in enumerate(reqs):
+        nb = cam.width * cam.height * 24
+        kind = i % 6
+        if kind in (0, 1):  # device memory, at 0 and 8 bytes into an allocation
+            b = ctx.alloc(nb + 16)
+            ptr = b.ptr + 8 * kind
+            read = (lambda b=b, k=kind, nb=nb: b.download(np.uint8, nb + 8 * k)[8 * k:])
+        elif kind in (2, 3, 4):  # page-locked host memory at 0, 8 and 4 bytes in
+            b = ctx.pinned(nb + 16)
+            off = (0, 8, 4)[kind - 2]
+            ptr = b.ptr + off
+            read = (lambda b=b, o=off, nb=nb: b.view(np.uint8, nb + o)[o:].copy())
+        else:  # pageable host memory
+            b = np.zeros(nb + 16, np.uint8)
+            ptr = b.ctypes.data
+            read = (lambda b=b, nb=nb: b[:nb].copy())
+        keep.append(b)
+        dsts.append(read)
+        srv.submit(sc, cam, shadow=shadow, tag=i, dst=ptr)
+    srv.drain()
+    comp = {c.user_tag: c for c in srv.poll()}
+    srv.close()
+    for i, (sc, cam, shadow, _) in enumerate(reqs):
+        c = comp[i]
+        assert c.status == 0
+        direct = ctx.raymarch(scenes[sc], cam, shadow=shadow)
+        got = dsts[i]()
+        assert np.array_equal(got, direct.view(np.uint8).reshape(-1)), f"request {i} (kind {i % 6})"
+        assert c.hit_checksum == meso.hit_checksum(direct)
+        assert c.n_rays == cam.width * cam.height + np.count_nonzero(direct["shadow_steps"])
+
+
 def test_edits_serialised_per_scene(ctx):
     reqs = _requests(2)
     assert any(r[3] for r in reqs)
