@@ -18,14 +18,14 @@ constexpr uint32_t kFull = 0xFFFFFFFFu;
 
 // ------------------------------------------------------------ vertices
 // Plane axes per face direction: X faces u=y v=z; Y faces u=x v=z; Z faces u=x v=y.
-// One thread per vertex (4 per quad), so a warp stores 512 contiguous bytes.
-__global__ void quads_to_vertices_kernel(const uint64_t* quads, uint64_t n, const int32_t* origins,
-                                         uint32_t n_chunks, meso_vertex* out, uint32_t* err) {
-  const uint64_t vi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  const uint64_t i = vi >> 2;
-  const int k = (int)(vi & 3u);
-  if (i >= n) return;
-  const uint64_t q = quads[i];
+// A CTA of kQvThreads threads writes kQvPer x kQvThreads consecutive
+// vertices (4 per quad); in step k thread t makes vertex
+// base + k*kQvThreads + t, so every warp store covers 512 contiguous bytes,
+// and a thread's kQvPer quad loads are issued before any of them is used.
+constexpr int kQvThreads = 256, kQvPer = 8;
+
+__device__ __forceinline__ float4 quad_vertex(uint64_t q, int k, const int32_t* origins, uint32_t n_chunks,
+                                              uint32_t* err) {
   const uint32_t chunk = (uint32_t)(q >> 44);
   const int dir = (int)((q >> 41) & 7u);
   const int lz = (int)((q >> 36) & 31u), ly = (int)((q >> 31) & 31u), lx = (int)((q >> 26) & 31u);
@@ -33,9 +33,9 @@ __global__ void quads_to_vertices_kernel(const uint64_t* quads, uint64_t n, cons
   const uint32_t mat = (uint32_t)(q & 0xFFFFu);
   int ox = 0, oy = 0, oz = 0;
   if (chunk < n_chunks) {
-    ox = origins[3 * chunk] * 32;
-    oy = origins[3 * chunk + 1] * 32;
-    oz = origins[3 * chunk + 2] * 32;
+    ox = __ldg(origins + 3 * chunk) * 32;
+    oy = __ldg(origins + 3 * chunk + 1) * 32;
+    oz = __ldg(origins + 3 * chunk + 2) * 32;
   } else if (k == 0) {
     atomicOr(err, ERR_BAD_INPUT);
   }
@@ -63,7 +63,25 @@ __global__ void quads_to_vertices_kernel(const uint64_t* quads, uint64_t n, cons
   vtx.y = (float)(oy + y);
   vtx.z = (float)(oz + z);
   vtx.w = __uint_as_float(mat | (uint32_t)dir << 16 | (uint32_t)k << 19);
-  reinterpret_cast<float4*>(out)[vi] = vtx;
+  return vtx;
+}
+
+__global__ void __launch_bounds__(kQvThreads) quads_to_vertices_kernel(const uint64_t* __restrict__ quads, uint64_t n,
+                                                                     const int32_t* __restrict__ origins,
+                                                                     uint32_t n_chunks, meso_vertex* __restrict__ out,
+                                                                     uint32_t* err) {
+  const uint64_t base = (uint64_t)blockIdx.x * (kQvPer * kQvThreads) + threadIdx.x;
+  uint64_t q[kQvPer];
+#pragma unroll
+  for (int k = 0; k < kQvPer; k++) {
+    const uint64_t i = (base + (uint64_t)k * kQvThreads) >> 2;
+    q[k] = i < n ? __ldg(quads + i) : 0ull;
+  }
+#pragma unroll
+  for (int k = 0; k < kQvPer; k++) {
+    const uint64_t vi = base + (uint64_t)k * kQvThreads;
+    if ((vi >> 2) < n) __stcs(reinterpret_cast<float4*>(out) + vi, quad_vertex(q[k], (int)(vi & 3u), origins, n_chunks, err));
+  }
 }
 
 // ------------------------------------------------------------ erosion
@@ -110,7 +128,11 @@ __device__ __forceinline__ bool chunk_voxel(const ErodeParams& p, uint32_t c, in
 // One CTA (256 threads) per chunk.  Mip d from mip d-1 on bit rows (z, y):
 // (R << 1) & (R >> 1) covers the two x neighbours of the own row, and
 // Q & (Q << 1) & (Q >> 1) the three x positions of each of the 8 other rows.
-__global__ void __launch_bounds__(256) erode_kernel(const ErodeParams p) {
+constexpr int kErodeThreads = 256;
+constexpr int kErodeBatch = 8;  // 16-byte loads a thread has in flight at once
+static_assert(4096 % (kErodeBatch * kErodeThreads) == 0, "a uint16 chunk is whole batches of loads");
+
+__global__ void __launch_bounds__(kErodeThreads) erode_kernel(const ErodeParams p) {
   __shared__ uint32_t mip0[1024], cur[1024], nxt[1024];
   const uint32_t c = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -135,26 +157,35 @@ __global__ void __launch_bounds__(256) erode_kernel(const ErodeParams p) {
     return;
   }
   if (p.kind == MESO_SRC_CHUNKS_U16 || p.kind == MESO_SRC_CHUNKS_U8) {
-    // contiguous chunk: 16-byte loads, each giving the occupancy bits of 8
-    // (uint16) or 16 (uint8) consecutive voxels of a row, written to the
-    // row word in shared memory as a byte or a half word (bit x = voxel x)
+    // contiguous chunk: 16-byte streaming loads, kErodeBatch per thread in
+    // flight at once, each giving the occupancy bits of 8 (uint16) or 16
+    // (uint8) consecutive voxels of a row, written to the row word in shared
+    // memory as a byte or a half word (bit x = voxel x)
     const uint32_t idx = p.coords ? (uint32_t)p.coords[c] : c;
     if (p.kind == MESO_SRC_CHUNKS_U16) {
       const uint4* src = reinterpret_cast<const uint4*>(p.data + (size_t)idx * 65536u);
       uint8_t* dst = reinterpret_cast<uint8_t*>(mip0);
-      for (int i = threadIdx.x; i < 4096; i += blockDim.x) {
-        const uint4 v = __ldg(src + i);
-        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-        uint32_t b = 0;
 #pragma unroll
-        for (int k = 0; k < 4; k++) b |= ((w[k] & 0xFFFFu) != 0 ? 1u : 0u) << (2 * k) | ((w[k] >> 16) != 0 ? 2u : 0u) << (2 * k);
-        dst[i] = (uint8_t)b;
+      for (int i0 = 0; i0 < 4096; i0 += kErodeBatch * kErodeThreads) {
+        uint4 v[kErodeBatch];
+#pragma unroll
+        for (int j = 0; j < kErodeBatch; j++) v[j] = __ldcs(src + i0 + j * kErodeThreads + threadIdx.x);
+#pragma unroll
+        for (int j = 0; j < kErodeBatch; j++) {
+          const uint32_t w[4] = {v[j].x, v[j].y, v[j].z, v[j].w};
+          uint32_t b = 0;
+#pragma unroll
+          for (int k = 0; k < 4; k++)
+            b |= ((w[k] & 0xFFFFu) != 0 ? 1u : 0u) << (2 * k) | ((w[k] >> 16) != 0 ? 2u : 0u) << (2 * k);
+          dst[i0 + j * kErodeThreads + threadIdx.x] = (uint8_t)b;
+        }
       }
     } else {
       const uint4* src = reinterpret_cast<const uint4*>(p.data + (size_t)idx * 32768u);
       uint16_t* dst = reinterpret_cast<uint16_t*>(mip0);
-      for (int i = threadIdx.x; i < 2048; i += blockDim.x) {
-        const uint4 v = __ldg(src + i);
+#pragma unroll
+      for (int i = threadIdx.x; i < 2048; i += kErodeThreads) {
+        const uint4 v = __ldcs(src + i);
         const uint32_t w[4] = {v.x, v.y, v.z, v.w};
         uint32_t b = 0;
 #pragma unroll
@@ -165,7 +196,7 @@ __global__ void __launch_bounds__(256) erode_kernel(const ErodeParams p) {
       }
     }
   } else {
-    for (int row = warp; row < 1024; row += 8) {
+    for (int row = warp; row < 1024; row += kErodeThreads / 32) {
       const int z = row >> 5, y = row & 31;
       const uint32_t w = __ballot_sync(kFull, chunk_voxel(p, c, cx, cy, cz, lane, y, z));
       if (lane == 0) mip0[row] = w;
@@ -218,10 +249,11 @@ meso_status meso_quads_to_vertices(meso_ctx* ctx, const uint64_t* d_quads, uint6
   if (reinterpret_cast<uintptr_t>(d_out) & 15u)
     return fail(MESO_ERR_INVALID_ARG, "quads_to_vertices: output must be 16-byte aligned");
   const cudaStream_t st = pick_stream(ctx, stream);
-  const uint64_t blocks = (4 * n + 255) / 256;
+  const uint64_t per_block = (uint64_t)kQvPer * kQvThreads;
+  const uint64_t blocks = (4 * n + per_block - 1) / per_block;
   if (blocks > 0x7FFFFFFFull) return fail(MESO_ERR_INVALID_ARG, "quads_to_vertices: too many quads");
-  quads_to_vertices_kernel<<<(unsigned)blocks, 256, 0, st>>>(d_quads, n, d_origins, n_chunks, d_out,
-                                                             ctx->d_scratch + 1);
+  quads_to_vertices_kernel<<<(unsigned)blocks, kQvThreads, 0, st>>>(d_quads, n, d_origins, n_chunks, d_out,
+                                                                    ctx->d_scratch + 1);
   ctx->launches.fetch_add(1);
   MESO_CUDA_TRY(cudaGetLastError());
   return MESO_OK;
@@ -264,7 +296,7 @@ meso_status meso_erode_mips(meso_ctx* ctx, const meso_mesh_source* src, const in
   } else {
     return fail(MESO_ERR_INVALID_ARG, "erode_mips: unknown source kind");
   }
-  erode_kernel<<<n, 256, 0, pick_stream(ctx, stream)>>>(p);
+  erode_kernel<<<n, kErodeThreads, 0, pick_stream(ctx, stream)>>>(p);
   ctx->launches.fetch_add(1);
   MESO_CUDA_TRY(cudaGetLastError());
   return MESO_OK;
