@@ -57,7 +57,9 @@ typedef struct meso_config {
   int32_t device;                 /* CUDA device ordinal */
   uint32_t mesh_ctas_per_sm;      /* persistent mesher CTAs (16 warps each) per SM, 1..2
                                      (0 = tuned/default 2) */
-  uint32_t mesh_chunks_per_ticket;/* chunks taken per queue ticket (0 = tuned/default 1) */
+  uint32_t mesh_chunks_per_ticket;/* chunks taken per queue ticket (0 = tuned/default 1); brick-map
+                                     sources size their tickets themselves (up to 8 chunks, tested
+                                     together against the scene's cell map) */
   uint32_t ray_tile_w, ray_tile_h;/* threads of one ray CTA tile (0 = tuned/default 8x4 per warp) */
   uint32_t ray_warps_per_cta;     /* 1..4, 0 = tuned/default */
   uint64_t hbm_budget_bytes;      /* admission budget for resident scenes + requests (0 = 90% of free) */
