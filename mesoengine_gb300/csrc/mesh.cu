@@ -920,13 +920,20 @@ __global__ void __launch_bounds__(kThreads, KindTraits<KIND>::kCtasPerSm)
             const uint32_t grow = Fr & Vr;  // faces that continue the row above in material
             bool active = is_start;
             int h = 1;
-            for (int r = v + 1; r < 32; r++) {
-              const uint32_t g = __shfl_sync(kFull, grow & ~cons, r);
-              const bool cont = active && (g & mask) == mask;
-              const uint32_t taken = __reduce_or_sync(kFull, cont ? mask : 0u);
-              if (lane == r) cons |= taken;
-              h += cont ? 1 : 0;
-              active = cont;
+            // two rows per step: row r+1's word is fetched with row r's (a
+            // row's consumed bits change only when its own turn comes)
+            for (int r = v + 1; r < 32; r += 2) {
+              const uint32_t gr = grow & ~cons;
+              const uint32_t g0 = __shfl_sync(kFull, gr, r);
+              const uint32_t g1 = __shfl_sync(kFull, gr, r + 1 < 32 ? r + 1 : 31);
+              const bool c0 = active && (g0 & mask) == mask;
+              const bool c1 = c0 && r + 1 < 32 && (g1 & mask) == mask;
+              const uint32_t t0 = __reduce_or_sync(kFull, c0 ? mask : 0u);
+              const uint32_t t1 = __reduce_or_sync(kFull, c1 ? mask : 0u);
+              if (lane == r) cons |= t0;
+              if (lane == r + 1) cons |= t1;
+              h += (c0 ? 1 : 0) + (c1 ? 1 : 0);
+              active = c1;
               if (!__any_sync(kFull, active)) break;
             }
             if (is_start) {
