@@ -471,7 +471,7 @@ def bench_mesh_brickmap(ctx, meso, scene, steps):
             "gvox_s": round(n * 32768 / (ms * 1e6), 2), "ms": round(ms, 4), "quads": quads, "bricks": bricks,
             "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
                          "frac": round(ach / hbm, 4), "algorithmic_bytes_per_launch": algo,
-                         "kernel": "mesh_kernel<BRICKMAP>"}}
+                         "traffic": ncu_traffic("mesh_kernel<BRICKMAP>"), "kernel": "mesh_kernel<BRICKMAP>"}}
 
 
 def cpu_mesh_baseline(m, n_single=512):
