@@ -190,10 +190,10 @@ def test_brickmap_chunks(ctx):
 
 
 def test_brickmap_counts_with_empty_repeated_and_bad_chunks(ctx):
-    """Brick-map chunks are taken from the queue 32 at a time and tested
-    against the scene's per-chunk occupancy: empty chunks get count 0 without
-    being meshed, repeated chunks are meshed again, and an out-of-range
-    coordinate gets count 0 and raises the invalid-argument flag."""
+    """A short list (one chunk per queue ticket): empty chunks get count 0
+    without being meshed, repeated chunks are meshed again, and an
+    out-of-range coordinate gets count 0 and raises the invalid-argument
+    flag."""
     t = meso.terrain_preset("small")
     scene = ctx.scene_from_terrain(t)
     bm = oracle.HostBrickMap.from_dense(scene.dense())
@@ -214,6 +214,35 @@ def test_brickmap_counts_with_empty_repeated_and_bad_chunks(ctx):
     remapped = (ref & np.uint64((1 << 44) - 1)) | (ok[chunk].astype(np.uint64) << np.uint64(44))
     assert np.array_equal(_sorted(q), np.sort(remapped))
     assert (counts == 0).sum() > 1  # empty chunks among them
+
+
+def test_brickmap_long_list_tickets(ctx):
+    """A list long enough that every CTA takes several list entries per
+    ticket (through a stride permutation of the list) and tests them
+    together against the scene's per-chunk cell map: 3,000 entries with
+    every chunk of the scene many times over, air chunks among them, and two
+    out-of-range coordinates.  Quads, per-entry counts and the flag equal
+    the oracle's, entry by entry."""
+    t = meso.terrain_preset("small")
+    scene = ctx.scene_from_terrain(t)
+    bm = oracle.HostBrickMap.from_dense(scene.dense())
+    allc = np.array([(x, y, z) for z in range(4) for y in range(4) for x in range(4)], dtype=np.int32)
+    rng = np.random.default_rng(17)
+    coords = allc[rng.integers(0, 64, 3000)]
+    bad = [777, 2222]
+    coords[bad[0]] = (4, 0, 0)
+    coords[bad[1]] = (0, -1, 0)
+    with pytest.raises(meso.MesoError, match="outside"):
+        ctx.mesh(meso.SRC_BRICKMAP, coords=coords, scene=scene)
+    q, counts = ctx.mesh(meso.SRC_BRICKMAP, coords=coords, scene=scene, chunk_counts=True, check=False)
+    ok = np.array([i for i in range(len(coords)) if i not in bad])
+    ref = oracle.mesh_chunks(oracle.SRC_BRICKMAP, coords=coords[ok], bm=bm)
+    chunk = (ref >> np.uint64(44)).astype(np.int64)
+    assert np.array_equal(counts[ok], np.bincount(chunk, minlength=len(ok)))
+    assert counts[bad[0]] == 0 and counts[bad[1]] == 0
+    remapped = (ref & np.uint64((1 << 44) - 1)) | (ok[chunk].astype(np.uint64) << np.uint64(44))
+    assert np.array_equal(_sorted(q), np.sort(remapped))
+    assert (counts[ok] == 0).sum() > 100  # air chunks among them
 
 
 def test_matches_golden_fixture(ctx):
