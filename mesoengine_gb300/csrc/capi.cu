@@ -535,7 +535,7 @@ meso_status meso_raymarch_host(meso_ctx* ctx, const meso_scene* scene, const mes
   if (!mapped) cudaGetLastError();
   if (mapped) {
     meso_status rc = launch_raymarch(ctx, &scene, cam, 1, light, flags, static_cast<meso_hit*>(pa.devicePointer), st,
-                                     nullptr, 0);
+                                     nullptr, 0, nullptr, nullptr, nullptr, true);
     cudaError_t e = cudaStreamSynchronize(st);
     if (rc == MESO_OK && e != cudaSuccess) rc = cuda_fail(e, "raymarch_host");
     return rc;

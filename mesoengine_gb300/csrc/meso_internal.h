@@ -129,13 +129,14 @@ struct RayView;
 // keeps the view's place in d_hits (views packed in order).  d_hash
 // (optional; at most kRayHashViews views, not with d_stats): the kernel adds
 // view v's order-sensitive hit checksum into d_hash[v] and its traced shadow
-// rays into d_hash[kRayHashViews + v].
+// rays into d_hash[kRayHashViews + v].  host_out: some output is
+// page-locked host memory, so the kernel writes whole rows of a CTA's pixels.
 constexpr uint32_t kRayHashViews = 64;
 meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* cams,
                             uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
                             cudaStream_t st, void* d_view_table, size_t view_table_bytes,
                             uint64_t* d_stats = nullptr, meso_hit* const* view_out = nullptr,
-                            unsigned long long* d_hash = nullptr);
+                            unsigned long long* d_hash = nullptr, bool host_out = false);
 size_t raymarch_view_table_bytes(uint32_t n_views);
 
 // Mesh store internals shared with the serving loop (store.cu).

@@ -73,6 +73,7 @@ struct RayParams {
   uint64_t* stats;
   unsigned long long* hash;  // checksum instantiation: [v] hit hash, [kRayHashViews + v] traced shadow rays
   uint32_t order_mul;  // CTA b takes block (b * order_mul) mod gridDim.x (0: block b)
+  uint32_t cta_rows;   // 1: the output is host memory; write whole CTA rows (see the kernel)
 };
 
 struct Trav {
@@ -537,11 +538,34 @@ __global__ void __launch_bounds__(128, 8) raymarch_kernel(const RayParams P, con
   __syncwarp();
   const uint32_t row_words = 3 * P.tile_w;
   uint64_t* base = reinterpret_cast<uint64_t*>(V.out);
+  // Output in host memory, a CTA of four 8x4 tiles side by side, all inside
+  // the image: after one barrier each warp writes one 32-pixel row of the
+  // CTA (768 contiguous bytes, whole 128-byte lines when the row starts on
+  // one), so no line crosses the CPU-GPU link in two pieces.  (Into device
+  // memory the barrier costs more than it saves.)
+  bool done = false;
+  if (P.cta_rows && warps == 4 && P.tile_w == 8 && P.tile_h == 4 && (bid + 1) * 4 <= P.total_tiles) {
+    const uint32_t x0 = px0 - 8u * (threadIdx.x >> 5);  // the CTA's first pixel column
+    const bool ok = (tx & 3u) == (threadIdx.x >> 5) && px0 + 8 <= V.width && py0 + 4 <= V.height &&
+                    ((reinterpret_cast<uintptr_t>(base) + (((uint64_t)py0 * V.width + x0) * 24)) & 15u) == 0 &&
+                    (V.width & 1u) == 0;
+    if (__syncthreads_and(ok)) {
+      const uint32_t row = threadIdx.x >> 5;
+      uint4* dst = reinterpret_cast<uint4*>(base + ((uint64_t)(py0 + row) * V.width + x0) * 3);
+#pragma unroll
+      for (int r = 0; r < 2; r++) {
+        const uint32_t c = (uint32_t)lane + 32u * r;  // 16-byte chunk c of the row (48 in all)
+        if (c < 48u) dst[c] = reinterpret_cast<const uint4*>(stage[c / 12u])[12u * row + c % 12u];
+      }
+      done = true;
+    }
+  }
   // a whole tile whose rows all start on 16 bytes goes out in 16-byte stores
   const bool vec = ((reinterpret_cast<uintptr_t>(base) + (((uint64_t)py0 * V.width + px0) * 24)) & 15u) == 0 &&
                    (V.width & 1u) == 0 && (P.tile_w & 1u) == 0 && px0 + P.tile_w <= V.width &&
                    py0 + P.tile_h <= V.height;
-  if (vec) {
+  if (done) {
+  } else if (vec) {
     const uint32_t row_vecs = row_words / 2;
 #pragma unroll
     for (int r = 0; r < 2; r++) {
@@ -684,7 +708,7 @@ static meso_status stage_view_table(const meso_scene* const* scenes, const meso_
 meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* cams,
                             uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
                             cudaStream_t st, void* d_view_table, size_t view_table_bytes, uint64_t* d_stats,
-                            meso_hit* const* view_out, unsigned long long* d_hash) {
+                            meso_hit* const* view_out, unsigned long long* d_hash, bool host_out) {
   if (!scenes || !cams || !d_hits) return fail(MESO_ERR_INVALID_ARG, "raymarch: null argument");
   if (n_views == 0) return MESO_OK;
   for (uint32_t v = 0; v < n_views; v++) {
@@ -714,6 +738,7 @@ meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, cons
     }
   P.stats = d_stats;
   P.hash = d_hash;
+  P.cta_rows = host_out ? 1u : 0u;
   static InlineViews empty_views;  // zero-initialised
   uint64_t tiles;
   if (n_views <= (uint32_t)kInlineViews) {

@@ -83,6 +83,7 @@ struct SrvRequest {
   double submit = 0;
   uint64_t pixels = 0;
   meso_hit* d_dst = nullptr;  // device address the kernel may store dst_hits through (null: copy)
+  bool dst_host = false;      // d_dst is page-locked host memory
 };
 
 struct Slot {
@@ -238,13 +239,14 @@ void launch_batch(meso_server* srv, Slot& s) {
   std::vector<const meso_scene*> scenes;
   std::vector<meso_camera> cams;
   std::vector<meso_hit*> view_out;
-  bool direct = false;
+  bool direct = false, host_out = false;
   uint64_t off = 0;
   for (auto& r : s.reqs) {
     scenes.push_back(srv->scenes[r.req.scene_index]);
     cams.push_back(r.req.camera);
     view_out.push_back(r.d_dst);
     direct = direct || r.d_dst;
+    host_out = host_out || r.dst_host;
     s.offsets.push_back(off);
     off += r.pixels;
   }
@@ -301,7 +303,7 @@ void launch_batch(meso_server* srv, Slot& s) {
   if (rc == MESO_OK)
     rc = launch_raymarch(ctx, scenes.data(), cams.data(), (uint32_t)cams.size(), srv->light, s.reqs[0].req.flags,
                          s.d_hits, rs, s.d_table, s.table_bytes, nullptr, direct ? view_out.data() : nullptr,
-                         s.d_sums);
+                         s.d_sums, host_out);
   if (rc == MESO_OK) {
     // delivery into the callers' buffers that the kernel could not store
     // into, before the completion is signalled
@@ -550,7 +552,10 @@ meso_status meso_server_submit(meso_server* srv, const meso_request* req, uint64
         dp = pa.devicePointer;
       else if (pa.type == cudaMemoryTypeHost)
         dp = pa.devicePointer;
-      if (dp && !(reinterpret_cast<uintptr_t>(dp) & 7u)) r.d_dst = static_cast<meso_hit*>(dp);
+      if (dp && !(reinterpret_cast<uintptr_t>(dp) & 7u)) {
+        r.d_dst = static_cast<meso_hit*>(dp);
+        r.dst_host = pa.type == cudaMemoryTypeHost;
+      }
     } else {
       cudaGetLastError();
     }

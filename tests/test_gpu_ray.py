@@ -115,12 +115,14 @@ def test_raymarch_host_entry(ctx, small):
     assert_hits_equal(ctx.raymarch_host(scene, cam), oracle.raymarch(bm, ocam))
 
 
-@pytest.mark.parametrize("height", [1, 389, 1100])
-def test_raymarch_host_pinned_direct(ctx, small, height):
+@pytest.mark.parametrize("w,height", [(40, 1), (40, 389), (40, 1100), (96, 72), (160, 37), (256, 256)])
+def test_raymarch_host_pinned_direct(ctx, small, w, height):
     # a page-locked output is written by the kernel directly (no device
-    # buffer, no copy); every byte of it must be overwritten
+    # buffer, no copy); every byte of it must be overwritten.  Widths that
+    # are multiples of 32 put four whole tiles side by side in most CTAs,
+    # which then write whole 32-pixel rows; the others (and the CTAs of the
+    # last, partial tile row) write tile by tile
     t, scene, bm = small
-    w = 40
     cam = meso.camera((-20.0, 150.0, 90.0), (64.0, 64.0, 10.0), w, height)
     ocam = oracle.camera((-20.0, 150.0, 90.0), (64.0, 64.0, 10.0), w, height)
     buf = ctx.pinned(w * height * meso.HIT_DTYPE.itemsize)
