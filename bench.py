@@ -428,8 +428,9 @@ def bench_ray_dense256(ctx, meso, grid, steps, flush):
 def bench_mesh_brickmap(ctx, meso, scene, steps):
     """Brick-map meshing: every 32^3 chunk of the 1024^3 terrain (32,768
     chunks, neighbours' faces seen across chunk borders) in one persistent
-    launch, materials staged brick by brick (1 KiB bulk copies of the
-    occupied bricks).  Algorithmic bytes: 4 B per pointer fetched (64 per
+    launch; air chunks are passed over by the scene's cell map, the occupied
+    bricks of the others staged by the whole CTA.  Algorithmic bytes: 4 B
+    per pointer fetched (64 per
     chunk), 1 KiB of materials + 64 B of occupancy per occupied brick, the
     one-voxel halo (6 x 32 x 32 occupancy bits per chunk) and 8 B per quad."""
     import ctypes
