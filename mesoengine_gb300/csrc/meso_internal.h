@@ -128,10 +128,15 @@ struct RayView;
 // device-mapped address aligned to 8 bytes; a null entry (or a null array)
 // keeps the view's place in d_hits (views packed in order).  d_hash
 // (optional; at most kRayHashViews views, not with d_stats): the kernel adds
-// view v's order-sensitive hit checksum into d_hash[v] and its traced shadow
-// rays into d_hash[kRayHashViews + v].  host_out: some output is
-// page-locked host memory, so the kernel writes whole rows of a CTA's pixels.
-constexpr uint32_t kRayHashViews = 64;
+// view v's order-sensitive hit checksum into the kRayHashSlots partial sums
+// d_hash[v * kRayHashSlots + s] and its traced shadow rays into
+// d_hash[kRayHashShadow + v * kRayHashSlots + s] (s = the CTA's index mod
+// kRayHashSlots, so that the warps' atomics spread over several addresses);
+// the caller adds the partial sums.  host_out: some output is page-locked
+// host memory, so the kernel writes whole rows of a CTA's pixels.
+constexpr uint32_t kRayHashViews = 64, kRayHashSlots = 8;
+constexpr uint32_t kRayHashShadow = kRayHashViews * kRayHashSlots;  // first shadow entry
+constexpr uint32_t kRayHashEntries = 2 * kRayHashShadow;
 meso_status launch_raymarch(meso_ctx* ctx, const meso_scene* const* scenes, const meso_camera* cams,
                             uint32_t n_views, const float light[3], uint32_t flags, meso_hit* d_hits,
                             cudaStream_t st, void* d_view_table, size_t view_table_bytes,

@@ -71,7 +71,7 @@ struct RayParams {
   float inv_light[3];  // 1 / light per axis, correctly rounded (0 for a zero component)
   uint32_t shadow;
   uint64_t* stats;
-  unsigned long long* hash;  // checksum instantiation: [v] hit hash, [kRayHashViews + v] traced shadow rays
+  unsigned long long* hash;  // checksum instantiation: partial sums per view (see launch_raymarch)
   uint32_t order_mul;  // CTA b takes block (b * order_mul) mod gridDim.x (0: block b)
   uint32_t cta_rows;   // 1: the output is host memory; write whole CTA rows (see the kernel)
 };
@@ -604,8 +604,9 @@ __global__ void __launch_bounds__(128, 8) raymarch_kernel(const RayParams P, con
     for (int o = 16; o; o >>= 1) term += __shfl_down_sync(kFullMask, term, o);
     shadow = __reduce_add_sync(kFullMask, shadow);
     if (lane == 0) {
-      atomicAdd(P.hash + lo, term);
-      atomicAdd(P.hash + kRayHashViews + lo, (unsigned long long)shadow);
+      const uint32_t slot = lo * kRayHashSlots + (bid & (kRayHashSlots - 1u));
+      atomicAdd(P.hash + slot, term);
+      if (shadow) atomicAdd(P.hash + kRayHashShadow + slot, (unsigned long long)shadow);
     }
   }
 }

@@ -54,6 +54,7 @@ namespace {
 
 constexpr uint32_t kMaxBatch = 64;
 static_assert(kMaxBatch == kRayHashViews, "the raymarch kernel sums checksums of at most one batch of views");
+constexpr uint32_t kQuadHash = kRayHashEntries, kQuadCount = kRayHashEntries + 1, kSums = kRayHashEntries + 2;
 
 __device__ __forceinline__ uint64_t mix64(uint64_t x) {
   // splitmix64 finaliser
@@ -97,7 +98,9 @@ struct Slot {
   uint64_t hit_cap = 0;  // pixels
   void* d_table = nullptr;
   size_t table_bytes = 0;
-  unsigned long long* d_sums = nullptr;  // [0,64) hit hash, [64,128) shadows, [128] quad hash, [129] quad count
+  // [0, kRayHashEntries): the raymarch's partial hit hashes and shadow
+  // counts; then the quad hash and the quad count
+  unsigned long long* d_sums = nullptr;
   unsigned long long* h_sums = nullptr;  // pinned copy
   uint64_t* d_quads = nullptr;
   uint64_t quad_cap = 0;
@@ -235,7 +238,7 @@ void launch_batch(meso_server* srv, Slot& s) {
   s.launch_status = MESO_OK;
   s.offsets.clear();
   s.n_dirty = 0;
-  cudaMemsetAsync(s.d_sums, 0, sizeof(unsigned long long) * (2 * kMaxBatch + 2), st);
+  cudaMemsetAsync(s.d_sums, 0, sizeof(unsigned long long) * kSums, st);
   std::vector<const meso_scene*> scenes;
   std::vector<meso_camera> cams;
   std::vector<meso_hit*> view_out;
@@ -278,12 +281,12 @@ void launch_batch(meso_server* srv, Slot& s) {
       meso_mesh_output o;
       o.d_quads = s.d_quads;
       o.capacity = s.quad_cap;
-      o.d_quad_count = reinterpret_cast<uint64_t*>(s.d_sums + 2 * kMaxBatch + 1);
+      o.d_quad_count = reinterpret_cast<uint64_t*>(s.d_sums + kQuadCount);
       meso_mesh_store* store = srv->stores.empty() ? nullptr : srv->stores[r.req.scene_index];
       o.d_chunk_quad_counts = store ? s.d_counts : nullptr;
       rc = launch_mesh(ctx, &src, s.d_coords, n_dirty, &o, st, false);
       if (rc == MESO_OK) {
-        quad_hash_kernel<<<64, 256, 0, st>>>(s.d_quads, o.d_quad_count, s.quad_cap, s.d_sums + 2 * kMaxBatch);
+        quad_hash_kernel<<<64, 256, 0, st>>>(s.d_quads, o.d_quad_count, s.quad_cap, s.d_sums + kQuadHash);
         ctx->launches.fetch_add(1);
       }
       // the scene's resident mesh: the dirty chunks' new quads replace their
@@ -316,7 +319,7 @@ void launch_batch(meso_server* srv, Slot& s) {
       cudaEventRecord(s.joined, rs);
       cudaStreamWaitEvent(st, s.joined, 0);
     }
-    cudaMemcpyAsync(s.h_sums, s.d_sums, sizeof(unsigned long long) * (2 * kMaxBatch + 2), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(s.h_sums, s.d_sums, sizeof(unsigned long long) * kSums, cudaMemcpyDeviceToHost, st);
     if (srv->cfg.keep_hits) cudaMemcpyAsync(s.h_hits, s.d_hits, off * sizeof(meso_hit), cudaMemcpyDeviceToHost, st);
   }
   if (rc == MESO_OK) {
@@ -350,12 +353,17 @@ void finish_batch(meso_server* srv, Slot& s) {
     const SrvRequest& r = s.reqs[k];
     meso_completion c = make_completion(srv, r, s.launch_status, s.start);
     if (s.launch_status == MESO_OK) {
-      c.hit_checksum = s.h_sums[k];
-      c.n_rays = r.pixels + s.h_sums[kMaxBatch + k];
+      unsigned long long hh = 0, sh = 0;
+      for (uint32_t j = 0; j < kRayHashSlots; j++) {
+        hh += s.h_sums[k * kRayHashSlots + j];
+        sh += s.h_sums[kRayHashShadow + k * kRayHashSlots + j];
+      }
+      c.hit_checksum = hh;
+      c.n_rays = r.pixels + sh;
       if (s.edit) {
         c.n_dirty_chunks = s.n_dirty;
-        c.quad_checksum = s.h_sums[2 * kMaxBatch];
-        c.n_quads = s.n_dirty ? s.h_sums[2 * kMaxBatch + 1] : 0;
+        c.quad_checksum = s.h_sums[kQuadHash];
+        c.n_quads = s.n_dirty ? s.h_sums[kQuadCount] : 0;
         if (c.n_quads > s.quad_cap) c.status = MESO_ERR_OVERFLOW;
       }
     }
@@ -479,7 +487,7 @@ meso_status meso_server_create(meso_ctx* ctx, const meso_server_config* cfg, mes
   // per slot: hits, view table, sums, quads, coordinates
   const uint32_t coord_cap = std::min<uint32_t>(max_chunks, MESO_MAX_CHUNKS_PER_CALL);
   const uint64_t per_slot = srv->cfg.max_batch_rays * sizeof(meso_hit) + raymarch_view_table_bytes(kMaxBatch) +
-                            srv->cfg.max_edit_quads * 8 + 12ull * coord_cap + 4096 +
+                            srv->cfg.max_edit_quads * 8 + 12ull * coord_cap + sizeof(unsigned long long) * kSums +
                             (srv->cfg.keep_meshes ? 16ull * coord_cap : 0);
   const uint64_t budget = srv->cfg.hbm_budget_bytes ? srv->cfg.hbm_budget_bytes : ctx->budget_bytes;
   const uint64_t scene_bytes = ctx->scene_bytes.load() + store_bytes;
@@ -501,8 +509,8 @@ meso_status meso_server_create(meso_ctx* ctx, const meso_server_config* cfg, mes
     s.hit_cap = srv->cfg.max_batch_rays;
     s.table_bytes = raymarch_view_table_bytes(kMaxBatch);
     if (e == cudaSuccess) e = cudaMalloc(&s.d_table, s.table_bytes);
-    if (e == cudaSuccess) e = cudaMalloc(&s.d_sums, sizeof(unsigned long long) * (2 * kMaxBatch + 2));
-    if (e == cudaSuccess) e = cudaMallocHost(&s.h_sums, sizeof(unsigned long long) * (2 * kMaxBatch + 2));
+    if (e == cudaSuccess) e = cudaMalloc(&s.d_sums, sizeof(unsigned long long) * kSums);
+    if (e == cudaSuccess) e = cudaMallocHost(&s.h_sums, sizeof(unsigned long long) * kSums);
     s.quad_cap = srv->cfg.max_edit_quads;
     if (e == cudaSuccess) e = cudaMalloc(&s.d_quads, s.quad_cap * 8);
     s.coord_cap = coord_cap;
