@@ -6,6 +6,10 @@
 //     Runtimes/Voxel/Chunk/ChunkPool.h:623-628)                              -> meso::Scene
 //   FChunkPool::PushToBlockPool (ChunkPool.h:381-445)                      -> meso::Scene::mesh
 //   the imposter draw (Samples/SimpleVoxel.cpp:374-393)                    -> meso::Scene::render
+//   chunk slots kept in the pools, replaced on regeneration
+//     (ChunkPool.h:446-622, upload :653-679)                               -> meso::MeshStore
+//   ThreadPool + TDoubleBufferQueue (Runtimes/Thread/ThreadPool.h:7-127,
+//     Runtimes/Thread/DoubleBufferQueue.h:4-51)                            -> meso::Server
 // Errors become meso::Error exceptions on the C++ side only; the C ABI below
 // never throws.
 #pragma once
@@ -94,6 +98,68 @@ class Scene {
  private:
   Context* ctx_;
   meso_scene* scene_ = nullptr;
+};
+
+// A scene's quads kept on the device: one arena plus a segment per chunk.
+class MeshStore {
+ public:
+  MeshStore(Context& ctx, const Scene& scene) : ctx_(&ctx) { check(meso_mesh_store_create(ctx.get(), scene.get(), &store_)); }
+  ~MeshStore() { meso_mesh_store_destroy(ctx_->get(), store_); }
+  MeshStore(const MeshStore&) = delete;
+  MeshStore& operator=(const MeshStore&) = delete;
+  meso_mesh_store* get() const { return store_; }
+
+  // Remeshes the chunks (linear chunk indices, e.g. Scene::edit's result)
+  // and replaces their segments.
+  void update(const std::vector<uint32_t>& chunks) {
+    check(meso_mesh_store_update(ctx_->get(), store_, chunks.data(), (uint32_t)chunks.size()));
+  }
+  // The chunks' quads into d_out (capacity quads); returns their count.
+  uint64_t gather(const std::vector<uint32_t>& chunks, uint64_t* d_out, uint64_t capacity) const {
+    uint64_t total = 0;
+    check(meso_mesh_store_gather(ctx_->get(), store_, chunks.data(), (uint32_t)chunks.size(), d_out, capacity,
+                                 &total));
+    return total;
+  }
+  meso_mesh_store_info info() const {
+    meso_mesh_store_info i{};
+    check(meso_mesh_store_get_info(ctx_->get(), store_, &i));
+    return i;
+  }
+
+ private:
+  Context* ctx_;
+  meso_mesh_store* store_ = nullptr;
+};
+
+// The serving loop over resident scenes: submit requests from any thread,
+// poll their completions.
+class Server {
+ public:
+  Server(Context& ctx, const std::vector<meso_scene*>& scenes, const meso_server_config& cfg = meso_server_config()) {
+    check(meso_server_create(ctx.get(), &cfg, scenes.data(), (uint32_t)scenes.size(), &srv_));
+  }
+  ~Server() { meso_server_destroy(srv_); }
+  Server(const Server&) = delete;
+  Server& operator=(const Server&) = delete;
+  meso_server* get() const { return srv_; }
+
+  uint64_t submit(const meso_request& req) {
+    uint64_t id = 0;
+    check(meso_server_submit(srv_, &req, &id));
+    return id;
+  }
+  std::vector<meso_completion> poll(uint32_t max = 1024) {
+    std::vector<meso_completion> out(max);
+    uint32_t n = 0;
+    check(meso_server_poll(srv_, out.data(), max, &n));
+    out.resize(n);
+    return out;
+  }
+  void drain(double timeout_s = 60.0) { check(meso_server_drain(srv_, timeout_s)); }
+
+ private:
+  meso_server* srv_ = nullptr;
 };
 
 }  // namespace meso

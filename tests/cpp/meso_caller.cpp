@@ -2,8 +2,10 @@
 // and libmeso_gb300.so the way a MesoEngine-style host would link it.  It
 // builds the 128^3 golden terrain, renders the golden 96x64 view and compares
 // the hits byte for byte with the golden file, meshes every chunk of the
-// scene, applies sphere edits and keeps a mesh store current, and writes the
-// quads it got (sorted) for the test to compare with the oracle.
+// scene, serves the golden view through the request loop (hits delivered
+// into page-locked host memory and into device memory, both compared byte
+// for byte), applies sphere edits and keeps a mesh store current, and
+// writes the quads it got (sorted) for the test to compare with the oracle.
 //
 //   meso_caller <camera.bin> <golden_hits.bin> <out_dir>
 // camera.bin: one meso_camera (72 bytes); golden_hits.bin: 96*64 meso_hit.
@@ -84,9 +86,45 @@ int main(int argc, char** argv) {
     ctx.sync();
     std::sort(quads.begin(), quads.end());
     write_file(std::string(argv[3]) + "/quads_before.bin", quads);
+    // the golden view served: one request delivered into page-locked host
+    // memory, one into device memory, both compared with the golden hits
+    {
+      meso::Server srv(ctx, {scene.get()});
+      void* h_dst = nullptr;
+      meso::check(meso_host_alloc_pinned(ctx.get(), golden.size(), &h_dst));
+      DevBuf d_dst(ctx, golden.size());
+      meso_request req{};
+      req.kind = MESO_REQ_RENDER;
+      req.scene_index = 0;
+      req.camera = cam;
+      req.flags = MESO_RAY_SHADOW;
+      req.dst_hits = static_cast<meso_hit*>(h_dst);
+      const uint64_t id_host = srv.submit(req);
+      req.dst_hits = static_cast<meso_hit*>(d_dst.p);
+      const uint64_t id_dev = srv.submit(req);
+      srv.drain();
+      const std::vector<meso_completion> done = srv.poll();
+      bool seen_host = false, seen_dev = false;
+      for (const meso_completion& c : done) {
+        if (c.status != MESO_OK) {
+          std::fprintf(stderr, "served request %llu failed: %d\n", (unsigned long long)c.request_id, c.status);
+          return 1;
+        }
+        seen_host = seen_host || c.request_id == id_host;
+        seen_dev = seen_dev || c.request_id == id_dev;
+      }
+      std::vector<char> served(golden.size());
+      meso::check(meso_memcpy_d2h(ctx.get(), served.data(), d_dst.p, served.size(), nullptr));
+      ctx.sync();
+      const bool host_ok = std::memcmp(h_dst, golden.data(), golden.size()) == 0;
+      meso::check(meso_host_free_pinned(ctx.get(), h_dst));
+      if (!seen_host || !seen_dev || !host_ok || served != golden) {
+        std::fprintf(stderr, "served hits differ from the golden file\n");
+        return 1;
+      }
+    }
     // edits, then the resident mesh store brought up to date
-    meso_mesh_store* store = nullptr;
-    meso::check(meso_mesh_store_create(ctx.get(), scene.get(), &store));
+    meso::MeshStore store(ctx, scene);
     std::vector<meso_sphere_edit> spheres;
     for (int k = 0; k < 12; k++) {
       meso_sphere_edit e{};
@@ -98,18 +136,21 @@ int main(int argc, char** argv) {
       spheres.push_back(e);
     }
     const std::vector<uint32_t> dirty = scene.edit(spheres);
-    meso::check(meso_mesh_store_update(ctx.get(), store, dirty.data(), (uint32_t)dirty.size()));
+    store.update(dirty);
     std::vector<uint32_t> all(64);
     for (uint32_t c = 0; c < 64; c++) all[c] = c;
-    uint64_t total = 0;
     DevBuf d_all(ctx, cap * 8);
-    meso::check(meso_mesh_store_gather(ctx.get(), store, all.data(), 64, static_cast<uint64_t*>(d_all.p), cap, &total));
+    const uint64_t total = store.gather(all, static_cast<uint64_t*>(d_all.p), cap);
+    if (store.info().live_quads != total) {
+      std::fprintf(stderr, "store holds %llu quads, gathered %llu\n", (unsigned long long)store.info().live_quads,
+                   (unsigned long long)total);
+      return 1;
+    }
     std::vector<uint64_t> after(total);
     meso::check(meso_memcpy_d2h(ctx.get(), after.data(), d_all.p, total * 8, nullptr));
     ctx.sync();
     std::sort(after.begin(), after.end());
     write_file(std::string(argv[3]) + "/quads_after.bin", after);
-    meso_mesh_store_destroy(ctx.get(), store);
     std::printf("ok: %llu quads, %zu dirty chunks, %llu quads after the edits\n", (unsigned long long)nq, dirty.size(),
                 (unsigned long long)total);
     return 0;
