@@ -560,29 +560,31 @@ __global__ void __launch_bounds__(128, 8) raymarch_kernel(const RayParams P, con
       done = true;
     }
   }
-  // a whole tile whose rows all start on 16 bytes goes out in 16-byte stores
-  const bool vec = ((reinterpret_cast<uintptr_t>(base) + (((uint64_t)py0 * V.width + px0) * 24)) & 15u) == 0 &&
-                   (V.width & 1u) == 0 && (P.tile_w & 1u) == 0 && px0 + P.tile_w <= V.width &&
-                   py0 + P.tile_h <= V.height;
-  if (done) {
-  } else if (vec) {
-    const uint32_t row_vecs = row_words / 2;
+  if (!done) {
+    // a whole tile whose rows all start on 16 bytes goes out in 16-byte
+    // stores, any other tile word by word
+    const bool vec = ((reinterpret_cast<uintptr_t>(base) + (((uint64_t)py0 * V.width + px0) * 24)) & 15u) == 0 &&
+                     (V.width & 1u) == 0 && (P.tile_w & 1u) == 0 && px0 + P.tile_w <= V.width &&
+                     py0 + P.tile_h <= V.height;
+    if (vec) {
+      const uint32_t row_vecs = row_words / 2;
 #pragma unroll
-    for (int r = 0; r < 2; r++) {
-      const uint32_t c = (uint32_t)lane + 32u * r;  // 16-byte chunk c of the tile (48 in all)
-      if (c < 48u) {
-        const uint32_t row = c / row_vecs, q = c % row_vecs;
-        const uint4 v = reinterpret_cast<const uint4*>(sw)[c];
-        reinterpret_cast<uint4*>(base + ((uint64_t)(py0 + row) * V.width + px0) * 3)[q] = v;
+      for (int r = 0; r < 2; r++) {
+        const uint32_t c = (uint32_t)lane + 32u * r;  // 16-byte chunk c of the tile (48 in all)
+        if (c < 48u) {
+          const uint32_t row = c / row_vecs, q = c % row_vecs;
+          const uint4 v = reinterpret_cast<const uint4*>(sw)[c];
+          reinterpret_cast<uint4*>(base + ((uint64_t)(py0 + row) * V.width + px0) * 3)[q] = v;
+        }
       }
-    }
-  } else {
+    } else {
 #pragma unroll
-    for (int r = 0; r < 3; r++) {
-      const uint32_t c = (uint32_t)lane + 32u * r;  // word c of the tile: row c / row_words
-      const uint32_t row = c / row_words, w = c % row_words;
-      const uint32_t x = px0 + w / 3, y = py0 + row;
-      if (x < V.width && y < V.height) base[((uint64_t)y * V.width + px0) * 3 + w] = sw[c];
+      for (int r = 0; r < 3; r++) {
+        const uint32_t c = (uint32_t)lane + 32u * r;  // word c of the tile: row c / row_words
+        const uint32_t row = c / row_words, w = c % row_words;
+        const uint32_t x = px0 + w / 3, y = py0 + row;
+        if (x < V.width && y < V.height) base[((uint64_t)y * V.width + px0) * 3 + w] = sw[c];
+      }
     }
   }
   if (kStats) {
