@@ -314,9 +314,31 @@ def bench_mesh(ctx, meso, steps, warmup):
     g.destroy()
     vox = MESH_CHUNKS * 32768
     algo = MESH_CHUNKS * 65536 + 8 * quads
+    # end to end through the host entry point: the chunks in page-locked host
+    # memory, the quads written back into page-locked host memory, every step
+    h_in = ctx.pinned(MESH_CHUNKS * 65536)
+    meso._check(L.meso_memcpy_d2h(ctx.handle, h_in.ptr, data.ptr, MESH_CHUNKS * 65536, None))
+    ctx.sync()
+    h_out = ctx.pinned(cap * 8)
+
+    def host_call():
+        meso._check(L.meso_mesh_host(ctx.handle, meso.SRC_CHUNKS_U16, h_in.ptr, MESH_CHUNKS, 0, 0, None,
+                                     MESH_CHUNKS, h_out.ptr, cap, ctypes.byref(total)))
+
+    for _ in range(2):
+        host_call()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        host_call()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / steps
+    assert int(total.value) == quads
+    dev_q = np.sort(qbuf.download(np.uint64, quads))
+    e2e_exact = bool(np.array_equal(np.sort(h_out.view(np.uint64, quads)), dev_q))
+    h_in.free()
+    h_out.free()
     return {"ms": ms, "ms_plain": ms_plain, "quads": quads, "gvox_s": vox / (ms * 1e6),
             "gvox_s_plain": vox / (ms_plain * 1e6), "gvox_s_graph": vox / (ms_graph * 1e6),
-            "algo_bytes": algo, "data": data, "qbuf": qbuf}
+            "algo_bytes": algo, "data": data, "qbuf": qbuf, "e2e_ms": e2e_ms, "e2e_exact": e2e_exact}
 
 
 def bench_mesh_u8(ctx, meso, m, steps):
@@ -924,6 +946,11 @@ def run_ours(args, world, rank, local, dist):
             "per_chunk_launch_gvox_s": round(m["gvox_s_plain"], 3),
             "per_chunk_launch_graph_replay_gvox_s": round(m["gvox_s_graph"], 3),
             "batched_over_per_launch": round(m["ms_plain"] / m["ms"], 2),
+            "e2e": {"value": round(MESH_CHUNKS * 32768 / (m["e2e_ms"] * 1e6), 2), "unit": "Gvox/s",
+                    "ms": round(m["e2e_ms"], 4), "h2d_bytes_per_step": MESH_CHUNKS * 65536,
+                    "d2h_bytes_per_step": 8 * m["quads"] + 8, "same_quads_as_device_path": m["e2e_exact"],
+                    "api": "meso_mesh_host (chunks in page-locked host memory, uploaded in slices of 1024 while "
+                           "the previous slice is meshed; quads written by the kernel into page-locked host memory)"},
             "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
                          "frac": round(ach / hbm, 4), "algorithmic_bytes_per_launch": m["algo_bytes"],
                          "traffic": ncu_traffic("mesh_kernel<CHUNKS_U16>"), "kernel": "mesh_kernel<CHUNKS_U16>"},

@@ -235,9 +235,12 @@ meso_status meso_mesh_chunks_per_launch(meso_ctx* ctx, const meso_mesh_source* s
 meso_status meso_mesh_check(meso_ctx* ctx, const meso_mesh_output* out, void* stream, uint64_t* h_count);
 /* Host-buffer form for callers that hold no device memory: copies the
  * chunk array (kind CHUNKS_U16/U8; nx chunks, or n_chunks when nx is 0) or
- * grid to the device,
- * meshes, and copies the quads back.  *h_count receives the number of quads
- * (MESO_ERR_OVERFLOW if it exceeds capacity). */
+ * grid to the device, meshes, and returns the quads.  A contiguous chunk
+ * array of more than 1024 chunks goes up in slices of 1024, each meshed
+ * while the next one is copied; if h_quads is page-locked host memory the
+ * kernel writes the quads into it directly, else they are copied back.
+ * Quads carry the chunks' indices in the whole array.  *h_count receives the
+ * number of quads (MESO_ERR_OVERFLOW if it exceeds capacity). */
 meso_status meso_mesh_host(meso_ctx* ctx, int32_t kind, const void* h_data, int32_t nx, int32_t ny,
                            int32_t nz, const int32_t* h_chunk_coords, uint32_t n_chunks, uint64_t* h_quads,
                            uint64_t capacity, uint64_t* h_count);

@@ -426,6 +426,115 @@ meso_status meso_mesh_check(meso_ctx* ctx, const meso_mesh_output* out, void* st
   return MESO_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// A contiguous host array of more than kHostSlice chunks is meshed in slices
+// of kHostSlice chunks: the upload of slice i+1 (a second stream) overlaps
+// the mesh launch of slice i, two device slice buffers in turn, and the
+// launches append to one quad buffer with the chunks' indices in the whole
+// array.  When h_quads is device-mapped page-locked memory the kernel writes
+// the quads into it directly, over the CPU-GPU link while the next slice
+// comes in the other way; otherwise they are copied back at the end.  On
+// 4096 uint16 chunks with page-locked input and output: 2.11 ms in one
+// upload, launch and download; slices of 256 / 512 / 1024 chunks 2.02 /
+// 1.69 / 1.60 ms (a slice must fill the GPU's CTAs to mesh as fast as it
+// arrives).
+constexpr uint32_t kHostSlice = 1024;
+
+meso_status mesh_host_pipelined(meso_ctx* ctx, int32_t kind, const uint8_t* h_data, uint32_t n, uint64_t* h_quads,
+                                uint64_t capacity, uint64_t* h_count) {
+  if (capacity && !h_quads) return fail(MESO_ERR_INVALID_ARG, "mesh_host: capacity without buffer");
+  const size_t chunk_bytes = kind == MESO_SRC_CHUNKS_U16 ? 65536 : 32768;
+  const size_t slice_bytes = chunk_bytes * kHostSlice;
+  const cudaStream_t st = ctx->stream;
+  uint64_t* d_direct = nullptr;  // h_quads as the device sees it, if it can
+  if (h_quads && capacity) {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, h_quads) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer &&
+        !(reinterpret_cast<uintptr_t>(pa.devicePointer) & 7u))
+      d_direct = static_cast<uint64_t*>(pa.devicePointer);
+    else
+      cudaGetLastError();
+  }
+  cudaStream_t cs = nullptr;
+  cudaEvent_t copied[2] = {nullptr, nullptr}, used[2] = {nullptr, nullptr}, ready = nullptr;
+  uint8_t* d = nullptr;
+  meso_status rc = MESO_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+    e = cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&used[b], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+  // [0, 2 slices) inputs, then the count, then the quads unless written to host memory
+  const size_t off_count = 2 * slice_bytes, off_quads = off_count + 256;
+  const size_t total = off_quads + (d_direct ? 0 : capacity * 8);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d, total, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d + off_count, 0, 8, st);
+  if (e == cudaSuccess) e = cudaEventRecord(ready, st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ready, 0);  // the buffers exist before the first copy
+  if (e != cudaSuccess) rc = cuda_fail(e, "mesh_host: set-up");
+  meso_mesh_output o;
+  o.d_quads = d_direct ? d_direct : reinterpret_cast<uint64_t*>(d + off_quads);
+  o.capacity = capacity;
+  o.d_quad_count = reinterpret_cast<uint64_t*>(d + off_count);
+  o.d_chunk_quad_counts = nullptr;
+  for (uint32_t s0 = 0, i = 0; rc == MESO_OK && s0 < n; s0 += kHostSlice, i++) {
+    const uint32_t cnt = n - s0 < kHostSlice ? n - s0 : kHostSlice;
+    const int b = (int)(i & 1u);
+    uint8_t* buf = d + (size_t)b * slice_bytes;
+    if (i >= 2) e = cudaStreamWaitEvent(cs, used[b], 0);  // the launch of slice i-2 has read buf
+    if (e == cudaSuccess) e = cudaMemcpyAsync(buf, h_data + (size_t)s0 * chunk_bytes, cnt * chunk_bytes,
+                                              cudaMemcpyHostToDevice, cs);
+    if (e == cudaSuccess) e = cudaEventRecord(copied[b], cs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, copied[b], 0);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(e, "mesh_host: upload");
+      break;
+    }
+    meso_mesh_source src;
+    memset(&src, 0, sizeof(src));
+    src.kind = kind;
+    src.d_data = buf;
+    src.nx = (int32_t)cnt;
+    rc = launch_mesh(ctx, &src, nullptr, cnt, &o, st, false, s0, true);
+    if (rc == MESO_OK && (e = cudaEventRecord(used[b], st)) != cudaSuccess) rc = cuda_fail(e, "mesh_host: event");
+  }
+  uint64_t cnt = 0;
+  if (rc == MESO_OK) {
+    e = cudaMemcpyAsync(&cnt, o.d_quad_count, 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "mesh_host");
+  }
+  if (rc == MESO_OK && !d_direct && h_quads && capacity) {
+    const uint64_t k = cnt < capacity ? cnt : capacity;
+    e = cudaMemcpyAsync(h_quads, o.d_quads, k * 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "mesh_host download");
+  }
+  // everything issued on cs is ordered before work on st that has finished
+  // or been synchronized; wait for cs too before its buffers and events go
+  if (cs) cudaStreamSynchronize(cs);
+  if (d) cudaFreeAsync(d, st);
+  const meso_status sync_rc = meso_sync(ctx, st);
+  if (rc == MESO_OK) rc = sync_rc;
+  for (int b = 0; b < 2; b++) {
+    if (copied[b]) cudaEventDestroy(copied[b]);
+    if (used[b]) cudaEventDestroy(used[b]);
+  }
+  if (ready) cudaEventDestroy(ready);
+  if (cs) cudaStreamDestroy(cs);
+  if (h_count) *h_count = cnt;
+  if (rc == MESO_OK && cnt > capacity) rc = fail(MESO_ERR_OVERFLOW, "mesh_host: quad buffer too small");
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
 meso_status meso_mesh_host(meso_ctx* ctx, int32_t kind, const void* h_data, int32_t nx, int32_t ny, int32_t nz,
                            const int32_t* h_coords, uint32_t n, uint64_t* h_quads, uint64_t capacity,
                            uint64_t* h_count) {
@@ -448,6 +557,8 @@ meso_status meso_mesh_host(meso_ctx* ctx, int32_t kind, const void* h_data, int3
     default: return fail(MESO_ERR_INVALID_ARG, "mesh_host: brick-map sources are device-resident; use meso_mesh_chunks");
   }
   if (coord_bytes && !h_coords) return fail(MESO_ERR_INVALID_ARG, "mesh_host: grid source needs coordinates");
+  if ((kind == MESO_SRC_CHUNKS_U16 || kind == MESO_SRC_CHUNKS_U8) && !h_coords && n > kHostSlice)
+    return mesh_host_pipelined(ctx, kind, static_cast<const uint8_t*>(h_data), n, h_quads, capacity, h_count);
   cudaStream_t st = ctx->stream;
   uint8_t* d = nullptr;
   const size_t off_coords = (data_bytes + 255) & ~size_t(255);

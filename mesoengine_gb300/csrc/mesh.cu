@@ -1014,7 +1014,7 @@ meso_status launch_kind(meso_ctx* ctx, const MeshParams& base, const CUtensorMap
     for (uint32_t i = 0; i < n_chunks; i++) {
       MeshParams p = base;
       p.n_chunks = 1;
-      p.chunk_id_base = i;
+      p.chunk_id_base = base.chunk_id_base + i;
       p.use_queue = 0;
       if (kCoords3) p.coords = base.coords + 3 * (size_t)i;
       else if (base.coords) p.coords = base.coords + i;
@@ -1057,9 +1057,11 @@ meso_status launch_kind(meso_ctx* ctx, const MeshParams& base, const CUtensorMap
 }  // namespace
 
 meso_status launch_mesh(meso_ctx* ctx, const meso_mesh_source* src, const int32_t* d_coords, uint32_t n_chunks,
-                        const meso_mesh_output* out, cudaStream_t st, bool per_launch) {
+                        const meso_mesh_output* out, cudaStream_t st, bool per_launch, uint32_t chunk_id_base,
+                        bool accumulate) {
   if (!src || !out || !out->d_quad_count) return fail(MESO_ERR_INVALID_ARG, "mesh: null source/output");
-  if (n_chunks > MESO_MAX_CHUNKS_PER_CALL) return fail(MESO_ERR_INVALID_ARG, "mesh: more than 2^20 chunks");
+  if ((uint64_t)chunk_id_base + n_chunks > MESO_MAX_CHUNKS_PER_CALL)
+    return fail(MESO_ERR_INVALID_ARG, "mesh: more than 2^20 chunks");
   if (out->capacity && !out->d_quads) return fail(MESO_ERR_INVALID_ARG, "mesh: capacity without buffer");
   MeshParams p;
   memset(&p, 0, sizeof(p));
@@ -1072,6 +1074,7 @@ meso_status launch_mesh(meso_ctx* ctx, const meso_mesh_source* src, const int32_
   p.ticket = ctx->d_tickets + (ctx->next_ticket.fetch_add(1) % meso_ctx::kTicketRing);
   p.err = ctx->d_scratch + 1;
   p.per_ticket = ctx->tuning.mesh_chunks_per_ticket ? ctx->tuning.mesh_chunks_per_ticket : 1;
+  p.chunk_id_base = chunk_id_base;
   CUtensorMap tmap;
   memset(&tmap, 0, sizeof(tmap));
   const int kind = src->kind;
@@ -1109,7 +1112,7 @@ meso_status launch_mesh(meso_ctx* ctx, const meso_mesh_source* src, const int32_
       return fail(MESO_ERR_INVALID_ARG, "mesh: unknown source kind");
     }
   }
-  MESO_CUDA_TRY(cudaMemsetAsync(out->d_quad_count, 0, sizeof(uint64_t), st));
+  if (!accumulate) MESO_CUDA_TRY(cudaMemsetAsync(out->d_quad_count, 0, sizeof(uint64_t), st));
   if (n_chunks == 0) return MESO_OK;
   switch (kind) {
     case MESO_SRC_CHUNKS_U16: return launch_kind<MESO_SRC_CHUNKS_U16>(ctx, p, tmap, n_chunks, st, per_launch);

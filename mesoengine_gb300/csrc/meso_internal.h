@@ -121,8 +121,12 @@ meso_status rebuild_macro(meso_ctx* ctx, meso_scene* s, const uint32_t* d_cells,
                           uint32_t n3 = 0);
 
 // Kernel launchers (defined in the .cu files).
+// chunk_id_base: added to the list index in each quad's chunk field (the
+// chunks are entries chunk_id_base .. of a longer list); accumulate: the
+// output count is not zeroed first, so several launches append to one buffer.
 meso_status launch_mesh(meso_ctx* ctx, const meso_mesh_source* src, const int32_t* d_coords,
-                        uint32_t n_chunks, const meso_mesh_output* out, cudaStream_t st, bool per_launch);
+                        uint32_t n_chunks, const meso_mesh_output* out, cudaStream_t st, bool per_launch,
+                        uint32_t chunk_id_base = 0, bool accumulate = false);
 struct RayView;
 // view_out (optional, n_views entries): where view v's hits go, a device or
 // device-mapped address aligned to 8 bytes; a null entry (or a null array)

@@ -177,6 +177,38 @@ def test_mesh_host_entry(ctx):
     assert np.array_equal(_sorted(q), ref)
 
 
+def test_mesh_host_slices(ctx):
+    """A host chunk array longer than one slice (1024 chunks) is meshed in
+    slices whose uploads overlap the previous slice's launch; the quads carry
+    the chunks' indices in the whole array and equal the one-launch device
+    path's, with the output in pageable memory (copied back at the end) and
+    in page-locked memory (written by the kernel), for uint16 and uint8
+    chunks; a buffer too small reports the count it needed."""
+    import ctypes
+    n = 1300
+    dev, _ = ctx.generate_chunks_u16(n, seed0=7)
+    host16 = dev.download(np.uint16, n * 32768).reshape(n, 32, 32, 32)
+    ref16, _ = ctx.mesh(meso.SRC_CHUNKS_U16, dev, n=n)
+    ref16 = _sorted(ref16)
+    assert np.array_equal(_sorted(ctx.mesh_host(meso.SRC_CHUNKS_U16, host16)), ref16)
+    cap = len(ref16) + 100
+    pin = ctx.pinned(cap * 8)
+    total = ctypes.c_uint64()
+    meso._check(meso._lib.meso_mesh_host(ctx.handle, meso.SRC_CHUNKS_U16, host16.ctypes.data, n, 0, 0, None, n,
+                                         pin.ptr, cap, ctypes.byref(total)))
+    assert total.value == len(ref16)
+    assert np.array_equal(np.sort(pin.view(np.uint64, total.value)), ref16)
+    pin.free()
+    host8 = (host16 % 251).astype(np.uint8)
+    d8 = ctx.to_device(host8)
+    ref8, _ = ctx.mesh(meso.SRC_CHUNKS_U8, d8, n=n)
+    assert np.array_equal(_sorted(ctx.mesh_host(meso.SRC_CHUNKS_U8, host8)), _sorted(ref8))
+    small = np.empty(1000, dtype=np.uint64)
+    rc = meso._lib.meso_mesh_host(ctx.handle, meso.SRC_CHUNKS_U16, host16.ctypes.data, n, 0, 0, None, n,
+                                  small.ctypes.data, 1000, ctypes.byref(total))
+    assert rc == 4 and total.value == len(ref16)  # MESO_ERR_OVERFLOW with the count needed
+
+
 def test_brickmap_chunks(ctx):
     t = meso.terrain_preset("small")
     scene = ctx.scene_from_terrain(t)
