@@ -446,6 +446,7 @@ constexpr uint32_t kHostSlice = 1024;
 meso_status mesh_host_pipelined(meso_ctx* ctx, int32_t kind, const uint8_t* h_data, uint32_t n, uint64_t* h_quads,
                                 uint64_t capacity, uint64_t* h_count) {
   if (capacity && !h_quads) return fail(MESO_ERR_INVALID_ARG, "mesh_host: capacity without buffer");
+  if (n > MESO_MAX_CHUNKS_PER_CALL) return fail(MESO_ERR_INVALID_ARG, "mesh_host: more than 2^20 chunks");
   const size_t chunk_bytes = kind == MESO_SRC_CHUNKS_U16 ? 65536 : 32768;
   const size_t slice_bytes = chunk_bytes * kHostSlice;
   const cudaStream_t st = ctx->stream;
