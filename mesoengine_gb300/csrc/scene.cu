@@ -853,8 +853,12 @@ static void touched_cells(const int64_t (*lo)[3], const int64_t (*hi)[3], uint32
 // The bricks a set of sphere edits may change (the voxel boxes of the
 // spheres) and the chunks to remesh (the boxes grown by one voxel, whose
 // faces may change), both sorted by linear index.
+// The bricks and chunks the spheres' boxes touch, and the cells of 4^3, 16^3
+// and 64^3 bricks holding those bricks (each sorted, unique).  A cell holds a
+// touched brick iff the box overlaps it, so the cells come from the boxes
+// directly, at the cells' own granularity.
 static void edit_sets(const meso_scene* s, const meso_sphere_edit* sp, uint32_t n, std::vector<uint32_t>& bricks,
-                      std::vector<uint32_t>& chunks) {
+                      std::vector<uint32_t>& chunks, std::vector<uint32_t> (&cells)[3]) {
   const int64_t N[3] = {s->nx, s->ny, s->nz};
   std::vector<int64_t> box((size_t)n * 12);
   auto lo = reinterpret_cast<int64_t (*)[3]>(box.data());
@@ -871,6 +875,13 @@ static void edit_sets(const meso_scene* s, const meso_sphere_edit* sp, uint32_t 
   const int64_t B[3] = {s->bx, s->by, s->bz}, C[3] = {s->nx / 32, s->ny / 32, s->nz / 32};
   touched_cells(lo, hi, n, 3, B, bricks);
   touched_cells(clo, chi, n, 5, C, chunks);
+  for (int l = 0; l < 3; l++) {
+    // cells of (4^(l+1))^3 bricks: 2^(5+2l) voxels on a side, grids as the cell maps index them
+    const int64_t cell = 4ll << (2 * l);
+    const int64_t G[3] = {l == 0 ? s->bx / 4 : (s->bx + cell - 1) / cell, l == 0 ? s->by / 4 : (s->by + cell - 1) / cell,
+                          l == 0 ? s->bz / 4 : (s->bz + cell - 1) / cell};
+    touched_cells(lo, hi, n, 5 + 2 * l, G, cells[l]);
+  }
 }
 
 meso_status edit_spheres(meso_ctx* ctx, meso_scene* s, const meso_sphere_edit* h_sp, uint32_t n, uint32_t* h_dirty,
@@ -878,28 +889,13 @@ meso_status edit_spheres(meso_ctx* ctx, meso_scene* s, const meso_sphere_edit* h
   if (!s || (n && !h_sp)) return fail(MESO_ERR_INVALID_ARG, "edit: null argument");
   for (uint32_t i = 0; i < n; i++)
     if (h_sp[i].radius < 0 || h_sp[i].radius > 4096) return fail(MESO_ERR_INVALID_ARG, "edit: radius out of range");
-  std::vector<uint32_t> bricks, chunks;
-  edit_sets(s, h_sp, n, bricks, chunks);
+  std::vector<uint32_t> bricks, chunks, cells[3];
+  edit_sets(s, h_sp, n, bricks, chunks, cells);
   if (n_dirty) *n_dirty = (uint32_t)chunks.size();
   if (h_dirty) std::copy(chunks.begin(), chunks.begin() + std::min<size_t>(chunks.size(), dirty_cap), h_dirty);
   if (bricks.empty()) return chunks.size() > dirty_cap && h_dirty ? fail(MESO_ERR_OVERFLOW, "edit: dirty list overflow") : MESO_OK;
   const size_t nb = bricks.size();
-  // cells of 4^3, 16^3 and 64^3 bricks holding the touched bricks (sorted
-  // unique): only their emptiness bytes are recomputed
-  std::vector<uint32_t> cells[3];
-  const uint32_t BX = (uint32_t)s->bx, BY = (uint32_t)s->by;
-  const uint32_t gx[3] = {BX >> 2, (BX + 15) / 16, (BX + 63) / 64}, gy[3] = {BY >> 2, ((uint32_t)s->by + 15) / 16,
-                                                                          ((uint32_t)s->by + 63) / 64};
-  for (int l = 0; l < 3; l++) {
-    const int sh = 2 * (l + 1);
-    cells[l].reserve(nb);
-    for (uint32_t b : bricks) {
-      const uint32_t x = b % BX, y = (b / BX) % BY, z = b / (BX * BY);
-      cells[l].push_back((x >> sh) + gx[l] * ((y >> sh) + gy[l] * (z >> sh)));
-    }
-    std::sort(cells[l].begin(), cells[l].end());
-    cells[l].erase(std::unique(cells[l].begin(), cells[l].end()), cells[l].end());
-  }
+  // only the emptiness bytes of the cells holding touched bricks are recomputed
   // device scratch: [spheres | bricks | cells | cells2 | cells3] uploaded in
   // one copy, then the per-brick temporaries
   const size_t nc = cells[0].size(), nc2 = cells[1].size(), nc3 = cells[2].size();
