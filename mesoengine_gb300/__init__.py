@@ -600,7 +600,7 @@ class Context:
         total = sum(c.width * c.height for c in cams)
         if out is None:
             out = self.alloc(total * 24)
-        L = np.asarray(light_dir() if light is None else light, dtype=np.float32)
+        L = _light_arg(light)
         fn = _lib.meso_raymarch_per_view if per_view else _lib.meso_raymarch
         _check(fn(self.handle, sh, ca, len(cams), _np_ptr(L), RAY_SHADOW if shadow else 0, out.ptr, stream))
         if not download:
@@ -610,7 +610,7 @@ class Context:
 
     def raymarch_host(self, scene: Scene, cam: Camera, light=None, shadow=True, out_ptr=None) -> np.ndarray:
         """Host-buffer entry point; out_ptr (e.g. a PinnedBuffer.ptr) receives the hits."""
-        L = np.asarray(light_dir() if light is None else light, dtype=np.float32)
+        L = _light_arg(light)
         hits = None
         if out_ptr is None:
             hits = np.empty(cam.width * cam.height, dtype=HIT_DTYPE)
@@ -630,7 +630,7 @@ class Context:
         total = sum(c.width * c.height for c in cams)
         if out is None:
             out = self.alloc(total * 24)
-        L = np.asarray(light_dir() if light is None else light, dtype=np.float32)
+        L = _light_arg(light)
         counts = np.zeros(4, dtype=np.uint64)
         _check(_lib.meso_raymarch_stats(self.handle, sh, ca, len(cams), _np_ptr(L), RAY_SHADOW if shadow else 0,
                                         out.ptr, _np_ptr(counts)))
@@ -739,6 +739,20 @@ class Graph:
 def light_dir(v=(0.3, 0.5, 0.8)) -> np.ndarray:
     a = np.asarray(v, dtype=np.float64)
     return (a / np.linalg.norm(a)).astype(np.float32)
+
+
+_DEFAULT_LIGHT = None
+
+
+def _light_arg(light):
+    """The light direction as a float32 array (the default one built once)."""
+    global _DEFAULT_LIGHT
+    if light is None:
+        if _DEFAULT_LIGHT is None:
+            _DEFAULT_LIGHT = light_dir()
+            _DEFAULT_LIGHT.setflags(write=False)
+        return _DEFAULT_LIGHT
+    return np.asarray(light, dtype=np.float32)
 
 
 def camera(origin, target, width, height, fov_y_deg=60.0, up=(0.0, 0.0, 1.0)) -> Camera:
