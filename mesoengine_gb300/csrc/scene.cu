@@ -471,40 +471,49 @@ __global__ void macro_kernel(const uint32_t* ptr, int bx, int by, uint8_t* macro
   if (lane == 0) macro[m] = occupied ? 1 : 0;
 }
 
-// One thread per 16x16x16-brick cell: any occupied 4x4x4-brick child -> 1; a
-// cell that extends past the grid is marked 1 too, so no jump leaves the grid.
+// One warp per 16x16x16-brick cell: any occupied 4x4x4-brick child -> 1 (its
+// 64 children read two per lane, at once); a cell that extends past the grid
+// is marked 1 too, so no jump leaves the grid.
 __global__ void macro2_kernel(const uint8_t* macro, int bx, int by, int bz, uint8_t* macro2, const uint32_t* list,
                               uint32_t n) {
   const int m2x = (bx + 15) / 16, m2y = (by + 15) / 16, m2z = (bz + 15) / 16;
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (list ? n : (uint32_t)(m2x * m2y * m2z))) return;
-  const uint32_t i = list ? list[t] : t;
+  const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= (list ? n : (uint64_t)m2x * m2y * m2z)) return;
+  const uint32_t i = list ? list[w] : (uint32_t)w;
   const int cx = (int)(i % (uint32_t)m2x), cy = (int)((i / (uint32_t)m2x) % (uint32_t)m2y), cz = (int)(i / ((uint32_t)m2x * m2y));
   const int mx = bx / 4, my = by / 4, mz = bz / 4;
-  bool any = (cx + 1) * 4 > mx || (cy + 1) * 4 > my || (cz + 1) * 4 > mz;
-  for (int k = 0; k < 64 && !any; k++) {
-    const int x = cx * 4 + (k & 3), y = cy * 4 + ((k >> 2) & 3), z = cz * 4 + (k >> 4);
-    any = macro[(uint32_t)x + (uint32_t)mx * ((uint32_t)y + (uint32_t)my * (uint32_t)z)] != 0;
-  }
-  macro2[i] = any ? 1 : 0;
+  const bool edge = (cx + 1) * 4 > mx || (cy + 1) * 4 > my || (cz + 1) * 4 > mz;
+  bool any = false;
+  if (!edge)
+    for (int k = lane; k < 64; k += 32) {
+      const int x = cx * 4 + (k & 3), y = cy * 4 + ((k >> 2) & 3), z = cz * 4 + (k >> 4);
+      any |= macro[(uint32_t)x + (uint32_t)mx * ((uint32_t)y + (uint32_t)my * (uint32_t)z)] != 0;
+    }
+  const bool set = edge || __any_sync(0xFFFFFFFFu, any);
+  if (lane == 0) macro2[i] = set ? 1 : 0;
 }
 
-// One thread per 64x64x64-brick cell: any nonzero 16x16x16 child, or a cell
+// One warp per 64x64x64-brick cell: any nonzero 16x16x16 child, or a cell
 // extending past the grid -> 1.
 __global__ void macro3_kernel(const uint8_t* macro2, int bx, int by, int bz, uint8_t* macro3, const uint32_t* list,
                               uint32_t n) {
   const int m3x = (bx + 63) / 64, m3y = (by + 63) / 64, m3z = (bz + 63) / 64;
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (list ? n : (uint32_t)(m3x * m3y * m3z))) return;
-  const uint32_t i = list ? list[t] : t;
+  const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= (list ? n : (uint64_t)m3x * m3y * m3z)) return;
+  const uint32_t i = list ? list[w] : (uint32_t)w;
   const int cx = (int)(i % (uint32_t)m3x), cy = (int)((i / (uint32_t)m3x) % (uint32_t)m3y), cz = (int)(i / ((uint32_t)m3x * m3y));
   const int m2x = (bx + 15) / 16, m2y = (by + 15) / 16;
-  bool any = (cx + 1) * 64 > bx || (cy + 1) * 64 > by || (cz + 1) * 64 > bz;
-  for (int k = 0; k < 64 && !any; k++) {
-    const int x = cx * 4 + (k & 3), y = cy * 4 + ((k >> 2) & 3), z = cz * 4 + (k >> 4);
-    any = macro2[(uint32_t)x + (uint32_t)m2x * ((uint32_t)y + (uint32_t)m2y * (uint32_t)z)] != 0;
-  }
-  macro3[i] = any ? 1 : 0;
+  const bool edge = (cx + 1) * 64 > bx || (cy + 1) * 64 > by || (cz + 1) * 64 > bz;
+  bool any = false;
+  if (!edge)
+    for (int k = lane; k < 64; k += 32) {
+      const int x = cx * 4 + (k & 3), y = cy * 4 + ((k >> 2) & 3), z = cz * 4 + (k >> 4);
+      any |= macro2[(uint32_t)x + (uint32_t)m2x * ((uint32_t)y + (uint32_t)m2y * (uint32_t)z)] != 0;
+    }
+  const bool set = edge || __any_sync(0xFFFFFFFFu, any);
+  if (lane == 0) macro3[i] = set ? 1 : 0;
 }
 
 // ---------------------------------------------------------------- scene API
@@ -569,12 +578,12 @@ meso_status rebuild_macro(meso_ctx* ctx, meso_scene* s, const uint32_t* d_cells,
                                                                      cells);
   const uint64_t cells2 = d_cells2 ? n2 : n_macro2_of(s);
   if (cells2)
-    macro2_kernel<<<(unsigned)((cells2 + 255) / 256), 256, 0, st>>>(s->d_macro, s->bx, s->by, s->bz, s->d_macro2,
-                                                                     d_cells2, n2);
+    macro2_kernel<<<(unsigned)((cells2 * 32 + 255) / 256), 256, 0, st>>>(s->d_macro, s->bx, s->by, s->bz,
+                                                                          s->d_macro2, d_cells2, n2);
   const uint64_t cells3 = d_cells3 ? n3 : n_macro3_of(s);
   if (cells3)
-    macro3_kernel<<<(unsigned)((cells3 + 255) / 256), 256, 0, st>>>(s->d_macro2, s->bx, s->by, s->bz, s->d_macro3,
-                                                                     d_cells3, n3);
+    macro3_kernel<<<(unsigned)((cells3 * 32 + 255) / 256), 256, 0, st>>>(s->d_macro2, s->bx, s->by, s->bz,
+                                                                          s->d_macro3, d_cells3, n3);
   ctx->launches.fetch_add(3);
   MESO_CUDA_TRY(cudaGetLastError());
   return MESO_OK;
