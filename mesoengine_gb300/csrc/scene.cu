@@ -825,8 +825,12 @@ meso_status generate_chunks_u16(meso_ctx* ctx, uint32_t n, uint32_t seed0, uint1
 // of G cells.  Small sets are collected and sorted; when the boxes cover a
 // sizeable part of the grid, a bitmap over the grid is marked and scanned
 // instead, so the cost stays bounded by the grid size.
+// The cells (2^shift voxels on a side, grid G) that the boxes [lo, hi]
+// overlap, unique; sorted unless `any_order` (then sorted only when two boxes
+// share a cell: boxes that share none enumerate disjoint cells, and the
+// sort is the costly part for a few thousand cells).
 static void touched_cells(const int64_t (*lo)[3], const int64_t (*hi)[3], uint32_t n, int shift, const int64_t G[3],
-                          std::vector<uint32_t>& out) {
+                          std::vector<uint32_t>& out, bool any_order = false) {
   out.clear();
   uint64_t volume = 0;
   for (uint32_t i = 0; i < n; i++) {
@@ -854,8 +858,21 @@ static void touched_cells(const int64_t (*lo)[3], const int64_t (*hi)[3], uint32
     for (size_t w = 0; w < bits.size(); w++)
       for (uint64_t m = bits[w]; m; m &= m - 1) out.push_back((uint32_t)(w * 64 + (uint64_t)__builtin_ctzll(m)));
   } else {
-    std::sort(out.begin(), out.end());
-    out.erase(std::unique(out.begin(), out.end()), out.end());
+    bool shared = !any_order;
+    for (uint32_t i = 0; i < n && !shared; i++) {
+      if (lo[i][0] > hi[i][0] || lo[i][1] > hi[i][1] || lo[i][2] > hi[i][2]) continue;
+      for (uint32_t j = i + 1; j < n && !shared; j++) {
+        if (lo[j][0] > hi[j][0] || lo[j][1] > hi[j][1] || lo[j][2] > hi[j][2]) continue;
+        bool all = true;
+        for (int a = 0; a < 3; a++)
+          all = all && std::max(lo[i][a] >> shift, lo[j][a] >> shift) <= std::min(hi[i][a] >> shift, hi[j][a] >> shift);
+        shared = all;
+      }
+    }
+    if (shared) {
+      std::sort(out.begin(), out.end());
+      out.erase(std::unique(out.begin(), out.end()), out.end());
+    }
   }
 }
 
@@ -863,7 +880,7 @@ static void touched_cells(const int64_t (*lo)[3], const int64_t (*hi)[3], uint32
 // spheres) and the chunks to remesh (the boxes grown by one voxel, whose
 // faces may change), both sorted by linear index.
 // The bricks and chunks the spheres' boxes touch, and the cells of 4^3, 16^3
-// and 64^3 bricks holding those bricks (each sorted, unique).  A cell holds a
+// and 64^3 bricks holding those bricks (all unique; all but the bricks sorted).  A cell holds a
 // touched brick iff the box overlaps it, so the cells come from the boxes
 // directly, at the cells' own granularity.
 static void edit_sets(const meso_scene* s, const meso_sphere_edit* sp, uint32_t n, std::vector<uint32_t>& bricks,
@@ -882,7 +899,7 @@ static void edit_sets(const meso_scene* s, const meso_sphere_edit* sp, uint32_t 
       chi[i][a] = std::min<int64_t>((int64_t)sp[i].center[a] + sp[i].radius + 1, N[a] - 1);
     }
   const int64_t B[3] = {s->bx, s->by, s->bz}, C[3] = {s->nx / 32, s->ny / 32, s->nz / 32};
-  touched_cells(lo, hi, n, 3, B, bricks);
+  touched_cells(lo, hi, n, 3, B, bricks, /*any_order=*/true);  // the edit kernels take them in any order
   touched_cells(clo, chi, n, 5, C, chunks);
   for (int l = 0; l < 3; l++) {
     // cells of (4^(l+1))^3 bricks: 2^(5+2l) voxels on a side, grids as the cell maps index them
