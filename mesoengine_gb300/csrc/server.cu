@@ -254,6 +254,23 @@ void launch_batch(meso_server* srv, Slot& s) {
     off += r.pixels;
   }
   meso_status rc = MESO_OK;
+  const cudaStream_t rs = s.edit ? s.stream2 : st;  // the render's stream
+  bool rendered = false;  // work was issued on rs: st must join it before the batch completes
+  // the batch's render (one launch for all its views), then the copies into
+  // the callers' buffers that the kernel could not store into, before the
+  // completion is signalled
+  auto render = [&]() {
+    rendered = true;
+    rc = launch_raymarch(ctx, scenes.data(), cams.data(), (uint32_t)cams.size(), srv->light, s.reqs[0].req.flags,
+                         s.d_hits, rs, s.d_table, s.table_bytes, nullptr, direct ? view_out.data() : nullptr,
+                         s.d_sums, host_out);
+    if (rc != MESO_OK) return;
+    for (size_t k = 0; k < s.reqs.size(); k++) {
+      meso_hit* dst = s.reqs[k].req.dst_hits;
+      if (dst && !s.reqs[k].d_dst)
+        cudaMemcpyAsync(dst, s.d_hits + s.offsets[k], s.reqs[k].pixels * sizeof(meso_hit), cudaMemcpyDefault, rs);
+    }
+  };
   if (s.edit) {
     SrvRequest& r = s.reqs[0];
     meso_scene* scene = srv->scenes[r.req.scene_index];
@@ -261,8 +278,11 @@ void launch_batch(meso_server* srv, Slot& s) {
     rc = edit_spheres(ctx, scene, r.edits.data(), (uint32_t)r.edits.size(), srv->dirty.data(),
                       (uint32_t)srv->dirty.size(), &n_dirty, st);
     if (rc == MESO_OK) {
+      // the render needs only the edited scene: it is issued first, on the
+      // second stream, and the remesh runs beside it
       cudaEventRecord(s.forked, st);
       cudaStreamWaitEvent(s.stream2, s.forked, 0);
+      render();
     }
     if (rc == MESO_OK && n_dirty > s.coord_cap) rc = fail(MESO_ERR_OVERFLOW, "server: too many dirty chunks");
     if (rc == MESO_OK && n_dirty) {
@@ -301,24 +321,15 @@ void launch_batch(meso_server* srv, Slot& s) {
       }
     }
     s.n_dirty = n_dirty;
+  } else {
+    render();
   }
-  const cudaStream_t rs = s.edit ? s.stream2 : st;  // the render's stream
-  if (rc == MESO_OK)
-    rc = launch_raymarch(ctx, scenes.data(), cams.data(), (uint32_t)cams.size(), srv->light, s.reqs[0].req.flags,
-                         s.d_hits, rs, s.d_table, s.table_bytes, nullptr, direct ? view_out.data() : nullptr,
-                         s.d_sums, host_out);
+  if (s.edit && rendered) {
+    // whatever was issued on the render's stream completes before the batch
+    cudaEventRecord(s.joined, rs);
+    cudaStreamWaitEvent(st, s.joined, 0);
+  }
   if (rc == MESO_OK) {
-    // delivery into the callers' buffers that the kernel could not store
-    // into, before the completion is signalled
-    for (size_t k = 0; k < s.reqs.size(); k++) {
-      meso_hit* dst = s.reqs[k].req.dst_hits;
-      if (dst && !s.reqs[k].d_dst)
-        cudaMemcpyAsync(dst, s.d_hits + s.offsets[k], s.reqs[k].pixels * sizeof(meso_hit), cudaMemcpyDefault, rs);
-    }
-    if (s.edit) {
-      cudaEventRecord(s.joined, rs);
-      cudaStreamWaitEvent(st, s.joined, 0);
-    }
     cudaMemcpyAsync(s.h_sums, s.d_sums, sizeof(unsigned long long) * kSums, cudaMemcpyDeviceToHost, st);
     if (srv->cfg.keep_hits) cudaMemcpyAsync(s.h_hits, s.d_hits, off * sizeof(meso_hit), cudaMemcpyDeviceToHost, st);
   }
